@@ -1,0 +1,319 @@
+/*
+ * qmckl_gpu.h — C ABI of the GB300 (sm_103a) implementation of the QMCkl basis-evaluation
+ * path: electron-nucleus displacement, Gaussian shell radials with exponent-cutoff
+ * screening, Cartesian AO polynomial vgl, and the MO vgl contraction.
+ *
+ * Drop-in for the `*_device` context API of the reference library (qmckl_sycl,
+ * include/qmckl_gpu.hpp): same function names, argument lists, exit codes and error
+ * behaviour. Every array argument is a pointer that the GPU can reach (device memory,
+ * or host memory through unified addressing); the library copies what it keeps. Every
+ * call that launches work waits for it before returning, like the reference's
+ * `q.wait()`, unless the context was switched to asynchronous mode.
+ *
+ * The one signature change: contexts are created on a CUDA device ordinal (or on a
+ * caller-provided cudaStream_t) instead of a sycl::queue
+ * (reference: src/qmckl_context.cpp:187).
+ *
+ * Layouts are C index order, exactly as the reference indexes them:
+ *   ao_vgl [point][5][ao], ao_value [point][ao], mo_vgl [point][5][mo],
+ *   mo_value [point][mo], shell_vgl [point][5][shell]; component 0 is the value,
+ *   1..3 the gradient (x, y, z), 4 the Laplacian.
+ */
+#ifndef QMCKL_GPU_H
+#define QMCKL_GPU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- Types and exit codes (reference: include/qmckl_types.hpp:24-57,74,116) ---- */
+typedef int32_t qmckl_exit_code_device;
+typedef int64_t qmckl_context_device;
+
+#define QMCKL_NULL_CONTEXT_DEVICE ((qmckl_context_device)0)
+
+#define QMCKL_SUCCESS_DEVICE ((qmckl_exit_code_device)0)
+#define QMCKL_INVALID_ARG_1_DEVICE ((qmckl_exit_code_device)1)
+#define QMCKL_INVALID_ARG_2_DEVICE ((qmckl_exit_code_device)2)
+#define QMCKL_INVALID_ARG_3_DEVICE ((qmckl_exit_code_device)3)
+#define QMCKL_INVALID_ARG_4_DEVICE ((qmckl_exit_code_device)4)
+#define QMCKL_INVALID_ARG_5_DEVICE ((qmckl_exit_code_device)5)
+#define QMCKL_INVALID_ARG_6_DEVICE ((qmckl_exit_code_device)6)
+#define QMCKL_INVALID_ARG_7_DEVICE ((qmckl_exit_code_device)7)
+#define QMCKL_INVALID_ARG_8_DEVICE ((qmckl_exit_code_device)8)
+#define QMCKL_INVALID_ARG_9_DEVICE ((qmckl_exit_code_device)9)
+#define QMCKL_INVALID_ARG_10_DEVICE ((qmckl_exit_code_device)10)
+#define QMCKL_FAILURE_DEVICE ((qmckl_exit_code_device)101)
+#define QMCKL_ERRNO_DEVICE ((qmckl_exit_code_device)102)
+#define QMCKL_INVALID_CONTEXT_DEVICE ((qmckl_exit_code_device)103)
+#define QMCKL_ALLOCATION_FAILED_DEVICE ((qmckl_exit_code_device)104)
+#define QMCKL_DEALLOCATION_FAILED_DEVICE ((qmckl_exit_code_device)105)
+#define QMCKL_NOT_PROVIDED_DEVICE ((qmckl_exit_code_device)106)
+#define QMCKL_OUT_OF_BOUNDS_DEVICE ((qmckl_exit_code_device)107)
+#define QMCKL_ALREADY_SET_DEVICE ((qmckl_exit_code_device)108)
+#define QMCKL_INVALID_EXIT_CODE_DEVICE ((qmckl_exit_code_device)109)
+
+#define QMCKL_MAX_FUN_LEN_DEVICE 256
+#define QMCKL_MAX_MSG_LEN_DEVICE 1024
+
+/* Host allocation record (reference: include/qmckl_types.hpp:100-103). */
+typedef struct qmckl_memory_info_struct {
+  size_t size;
+  void* pointer;
+} qmckl_memory_info_struct_device;
+
+/* Containers, Fortran order: element (i, j) of a matrix is data[i + j*size[0]]
+ * (reference: include/qmckl_types.hpp:78-96). */
+typedef struct qmckl_vector_device {
+  double* data;
+  int64_t size;
+} qmckl_vector_device;
+typedef struct qmckl_matrix_device {
+  double* data;
+  int64_t size[2];
+} qmckl_matrix_device;
+#define QMCKL_TENSOR_ORDER_MAX_DEVICE 16
+typedef struct qmckl_tensor_device {
+  double* data;
+  int64_t order;
+  int64_t size[QMCKL_TENSOR_ORDER_MAX_DEVICE];
+} qmckl_tensor_device;
+
+/* ---- Context (reference: src/qmckl_context.cpp) ---- */
+/* replaces qmckl_context_create_device(sycl::queue), src/qmckl_context.cpp:187-288 */
+qmckl_context_device qmckl_context_create_device(int32_t device_id);
+/* same, but work is issued on the caller's cudaStream_t (passed as void*) */
+qmckl_context_device qmckl_context_create_with_stream_device(int32_t device_id, void* cuda_stream);
+/* src/qmckl_context.cpp:294-345: frees every registered allocation, invalidates the tag */
+qmckl_exit_code_device qmckl_context_destroy_device(const qmckl_context_device context);
+/* src/qmckl_context.cpp:64-79: the context itself if valid, else QMCKL_NULL_CONTEXT_DEVICE */
+qmckl_context_device qmckl_context_check_device(const qmckl_context_device context);
+/* src/qmckl_context.cpp:47-62: date += 1, point.date = date (invalidates every cached array) */
+qmckl_exit_code_device qmckl_context_touch_device(const qmckl_context_device context);
+/* src/qmckl_context.cpp:81-110 (recursive lock) */
+void qmckl_lock_device(qmckl_context_device context);
+void qmckl_unlock_device(qmckl_context_device context);
+
+/* ---- Errors (reference: src/qmckl_basic_functions.cpp) ---- */
+/* src/qmckl_basic_functions.cpp:12-40 */
+qmckl_exit_code_device qmckl_set_error_device(qmckl_context_device context, const qmckl_exit_code_device exit_code,
+                                              const char* function_name, const char* message);
+/* src/qmckl_basic_functions.cpp:51-78: records the error and returns exit_code */
+qmckl_exit_code_device qmckl_failwith_device(qmckl_context_device context, const qmckl_exit_code_device exit_code,
+                                             const char* function, const char* message);
+/* src/qmckl_basic_functions.cpp:42-48 (the reference's switch is empty; this one names each code) */
+const char* qmckl_string_of_error_device(const qmckl_exit_code_device error);
+/* Reads ctx->error (include/qmckl_types.hpp:59-65); function/message buffers may be NULL. */
+qmckl_exit_code_device qmckl_get_error_device(qmckl_context_device context, qmckl_exit_code_device* exit_code,
+                                              char* function, int64_t function_size, char* message,
+                                              int64_t message_size);
+
+/* ---- Memory (reference: src/qmckl_memory.cpp) ---- */
+/* src/qmckl_memory.cpp:15-65 */
+void* qmckl_malloc_host(qmckl_context_device context, const qmckl_memory_info_struct_device info);
+/* src/qmckl_memory.cpp:70-125: device allocation recorded in the context (zero-filled) */
+void* qmckl_malloc_device(qmckl_context_device context, size_t size);
+/* src/qmckl_memory.cpp:127-171 */
+qmckl_exit_code_device qmckl_free_host(qmckl_context_device context, void* const ptr);
+/* src/qmckl_memory.cpp:173-220: QMCKL_FAILURE_DEVICE if the pointer is not registered */
+qmckl_exit_code_device qmckl_free_device(qmckl_context_device context, void* const ptr);
+/* src/qmckl_memory.cpp:226-361: synchronous copies on the context's stream */
+qmckl_exit_code_device qmckl_memcpy_H2D(qmckl_context_device context, void* const dest, void* const src, size_t size);
+qmckl_exit_code_device qmckl_memcpy_D2H(qmckl_context_device context, void* const dest, void* const src, size_t size);
+qmckl_exit_code_device qmckl_memcpy_D2D(qmckl_context_device context, void* const dest, void* const src, size_t size);
+
+/* ---- Containers (reference: src/qmckl_blas.cpp:14-306) ---- */
+qmckl_vector_device qmckl_vector_alloc_device(qmckl_context_device context, const int64_t size);
+qmckl_exit_code_device qmckl_vector_free_device(qmckl_context_device context, qmckl_vector_device* vector);
+qmckl_exit_code_device qmckl_vector_of_double_device(const qmckl_context_device context, const double* target,
+                                                     const int64_t size_max, qmckl_vector_device* vector_out);
+qmckl_matrix_device qmckl_matrix_alloc_device(qmckl_context_device context, const int64_t size1, const int64_t size2);
+qmckl_exit_code_device qmckl_matrix_free_device(qmckl_context_device context, qmckl_matrix_device* matrix);
+qmckl_exit_code_device qmckl_matrix_of_double_device(const qmckl_context_device context, const double* target,
+                                                     const int64_t size_max, qmckl_matrix_device* matrix_out);
+qmckl_exit_code_device qmckl_transpose_device(qmckl_context_device context, const qmckl_matrix_device A,
+                                              qmckl_matrix_device At);
+qmckl_tensor_device qmckl_tensor_alloc_device(qmckl_context_device context, const int64_t order, const int64_t* size);
+qmckl_exit_code_device qmckl_tensor_free_device(qmckl_context_device context, qmckl_tensor_device* tensor);
+
+/* ---- Points (reference: src/qmckl_point.cpp) ---- */
+/* src/qmckl_point.cpp:68-135: 'N' = coord[num][3], 'T' = coord[3][num]; touches the context */
+qmckl_exit_code_device qmckl_set_point_device(qmckl_context_device context, char transp, int64_t num, double* coord,
+                                              int64_t size_max);
+/* src/qmckl_point.cpp:5-66 */
+qmckl_exit_code_device qmckl_get_point_device(const qmckl_context_device context, const char transp,
+                                              double* const coord, const int64_t size_max);
+
+/* ---- Nucleus (reference: src/qmckl_nucleus.cpp:359-663) ---- */
+bool qmckl_nucleus_provided_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_get_nucleus_num_device(qmckl_context_device context, int64_t* num);
+/* src/qmckl_nucleus.cpp:510-540: QMCKL_ALREADY_SET_DEVICE on a second call */
+qmckl_exit_code_device qmckl_set_nucleus_num_device(qmckl_context_device context, int64_t num);
+/* src/qmckl_nucleus.cpp:614-663 */
+qmckl_exit_code_device qmckl_set_nucleus_charge_device(qmckl_context_device context, double* charge,
+                                                       int64_t size_max);
+/* src/qmckl_nucleus.cpp:543-610: 'N' = coord[num][3], 'T' = coord[3][num] */
+qmckl_exit_code_device qmckl_set_nucleus_coord_device(qmckl_context_device context, char transp, double* coord,
+                                                      int64_t size_max);
+qmckl_exit_code_device qmckl_get_nucleus_coord_device(const qmckl_context_device context, const char transp,
+                                                      double* const coord, const int64_t size_max);
+qmckl_exit_code_device qmckl_get_nucleus_charge_device(const qmckl_context_device context, double* const charge,
+                                                       const int64_t size_max);
+
+/* ---- Electrons (reference: src/qmckl_electron.cpp:8-190) ---- */
+bool qmckl_electron_provided_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_set_electron_num_device(qmckl_context_device context, int64_t up_num, int64_t down_num);
+/* src/qmckl_electron.cpp:50-90: swaps the walker point sets, then set_point(walk_num*elec_num) */
+qmckl_exit_code_device qmckl_set_electron_coord_device(qmckl_context_device context, char transp, int64_t walk_num,
+                                                       double* coord, int64_t size_max);
+qmckl_exit_code_device qmckl_get_electron_num_device(const qmckl_context_device context, int64_t* const num);
+qmckl_exit_code_device qmckl_get_electron_coord_device(const qmckl_context_device context, const char transp,
+                                                       double* const coord, const int64_t size_max);
+
+/* ---- AO basis (reference: src/qmckl_ao.cpp, src/qmckl_ao_sycl.cpp) ---- */
+bool qmckl_ao_basis_provided_device(qmckl_context_device context); /* src/qmckl_ao.cpp:28-40 */
+/* Setters, src/qmckl_ao.cpp:402-1236. Each clears one bit of the 14-bit mask; the setter
+ * that clears the last bit runs the finalize step (src/qmckl_ao_sycl.cpp:1067-1236). */
+qmckl_exit_code_device qmckl_set_ao_basis_type_device(qmckl_context_device context, char basis_type);
+qmckl_exit_code_device qmckl_set_ao_basis_shell_num_device(qmckl_context_device context, int64_t shell_num);
+qmckl_exit_code_device qmckl_set_ao_basis_prim_num_device(qmckl_context_device context, int64_t prim_num);
+qmckl_exit_code_device qmckl_set_ao_basis_ao_num_device(qmckl_context_device context, int64_t ao_num);
+qmckl_exit_code_device qmckl_set_ao_basis_nucleus_index_device(qmckl_context_device context, int64_t* nucleus_index,
+                                                               int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_nucleus_shell_num_device(qmckl_context_device context,
+                                                                   int64_t* nucleus_shell_num, int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_shell_ang_mom_device(qmckl_context_device context, int32_t* shell_ang_mom,
+                                                               int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_shell_prim_num_device(qmckl_context_device context,
+                                                                int64_t* shell_prim_num, int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_shell_prim_index_device(qmckl_context_device context,
+                                                                  int64_t* shell_prim_index, int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_shell_factor_device(qmckl_context_device context, double* shell_factor,
+                                                              int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_exponent_device(qmckl_context_device context, double* exponent,
+                                                          int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_coefficient_device(qmckl_context_device context, double* coefficient,
+                                                             int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_prim_factor_device(qmckl_context_device context, double* prim_factor,
+                                                             int64_t size_max);
+qmckl_exit_code_device qmckl_set_ao_basis_ao_factor_device(qmckl_context_device context, double* ao_factor,
+                                                           int64_t size_max);
+/* Getters, src/qmckl_ao.cpp:1238-1765 */
+qmckl_exit_code_device qmckl_get_ao_basis_type_device(qmckl_context_device context, char* const basis_type);
+qmckl_exit_code_device qmckl_get_ao_basis_shell_num_device(qmckl_context_device context, int64_t* const shell_num);
+qmckl_exit_code_device qmckl_get_ao_basis_prim_num_device(qmckl_context_device context, int64_t* prim_num);
+qmckl_exit_code_device qmckl_get_ao_basis_ao_num_device(qmckl_context_device context, int64_t* ao_num);
+qmckl_exit_code_device qmckl_get_ao_basis_nucleus_shell_num_device(qmckl_context_device context,
+                                                                   int64_t* nucleus_shell_num, int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_nucleus_index_device(qmckl_context_device context, int64_t* nucleus_index,
+                                                               int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_shell_ang_mom_device(qmckl_context_device context, int32_t* shell_ang_mom,
+                                                               int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_shell_factor_device(qmckl_context_device context, double* shell_factor,
+                                                              int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_shell_prim_num_device(qmckl_context_device context,
+                                                                int64_t* shell_prim_num, int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_shell_prim_index_device(qmckl_context_device context,
+                                                                  int64_t* shell_prim_index, int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_exponent_device(qmckl_context_device context, double* exponent,
+                                                          int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_coefficient_device(qmckl_context_device context, double* coefficient,
+                                                             int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_prim_factor_device(qmckl_context_device context, double* prim_factor,
+                                                             int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_ao_factor_device(qmckl_context_device context, double* ao_factor,
+                                                           int64_t size_max);
+/* Derived tables of the finalize step, src/qmckl_ao_sycl.cpp:1087-1231 */
+qmckl_exit_code_device qmckl_get_ao_basis_nucleus_range_device(qmckl_context_device context, double* nucleus_range,
+                                                               int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_nucleus_max_ang_mom_device(qmckl_context_device context,
+                                                                     int32_t* nucleus_max_ang_mom, int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_coefficient_normalized_device(qmckl_context_device context,
+                                                                        double* coefficient_normalized,
+                                                                        int64_t size_max);
+/* Provides (lazy, date-stamped), src/qmckl_ao.cpp:47-199, src/qmckl_ao_sycl.cpp:748-849 */
+qmckl_exit_code_device qmckl_provide_ao_basis_shell_vgl_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_provide_ao_basis_ao_vgl_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_provide_ao_basis_ao_value_device(qmckl_context_device context);
+/* Results, src/qmckl_ao.cpp:207-396 */
+qmckl_exit_code_device qmckl_get_ao_basis_shell_vgl_device(qmckl_context_device context, double* const shell_vgl,
+                                                           const int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_ao_vgl_device(qmckl_context_device context, double* const ao_vgl,
+                                                        const int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_ao_vgl_inplace_device(qmckl_context_device context, double* const ao_vgl,
+                                                                const int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_ao_value_device(qmckl_context_device context, double* const ao_value,
+                                                          const int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_ao_value_inplace_device(qmckl_context_device context,
+                                                                  double* const ao_value, const int64_t size_max);
+
+/* ---- MO basis (reference: src/qmckl_mo.cpp, src/qmckl_mo_sycl.cpp) ---- */
+bool qmckl_mo_basis_provided_device(qmckl_context_device context); /* src/qmckl_mo.cpp:10-23 */
+qmckl_exit_code_device qmckl_get_mo_basis_mo_num_device(qmckl_context_device context, int64_t* mo_num);
+/* src/qmckl_mo.cpp:487-524 and :527-583: QMCKL_ALREADY_SET_DEVICE on a second call.
+ * coefficient is [mo_num][ao_num]. */
+qmckl_exit_code_device qmckl_set_mo_basis_mo_num_device(qmckl_context_device context, int64_t mo_num);
+qmckl_exit_code_device qmckl_set_mo_basis_coefficient_device(qmckl_context_device context, double* coefficient);
+/* src/qmckl_mo.cpp:31-106: keep[] is a HOST array of mo_num flags */
+bool qmckl_mo_basis_select_mo_device(qmckl_context_device context, int32_t* keep, int64_t size_max);
+qmckl_exit_code_device qmckl_provide_mo_basis_mo_vgl_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_device context);
+/* src/qmckl_mo.cpp:294-453 */
+qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device context, double* const mo_vgl,
+                                                        const int64_t size_max);
+qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_inplace_device(qmckl_context_device context, double* const mo_vgl,
+                                                                const int64_t size_max);
+qmckl_exit_code_device qmckl_get_mo_basis_mo_value_device(qmckl_context_device context, double* const mo_value,
+                                                          const int64_t size_max);
+qmckl_exit_code_device qmckl_get_mo_basis_mo_value_inplace_device(qmckl_context_device context,
+                                                                  double* const mo_value, const int64_t size_max);
+
+/* ======================================================================================
+ * GB300 extensions (no counterpart in the reference; the reference behaviour is the
+ * default of each).
+ * ====================================================================================== */
+
+/* MO contraction precision. FP64 (default, the drop-in) or a split-BF16 product on the
+ * tcgen05 tensor cores (each FP64 operand split into three BF16 terms, six cross
+ * products, FP32 accumulation folded into FP64). Distances, exponentials, screening and
+ * the AO Laplacian assembly stay FP64 in both modes. Changing the mode touches the
+ * context. */
+#define QMCKL_PRECISION_FP64_DEVICE 0
+#define QMCKL_PRECISION_SPLIT_BF16_DEVICE 1
+qmckl_exit_code_device qmckl_set_precision_mode_device(qmckl_context_device context, int32_t mode);
+qmckl_exit_code_device qmckl_get_precision_mode_device(qmckl_context_device context, int32_t* mode);
+
+/* Asynchronous mode: when on, calls return after enqueueing their work on the
+ * context's stream (no host wait). Off by default (the reference waits on every call). */
+qmckl_exit_code_device qmckl_set_async_device(qmckl_context_device context, int32_t async);
+/* The cudaStream_t the context issues its work on (as void*). */
+void* qmckl_get_stream_device(qmckl_context_device context);
+/* Waits for all work issued by the context. */
+qmckl_exit_code_device qmckl_synchronize_device(qmckl_context_device context);
+
+/* Kernel timing: when enabled, every kernel the context launches is bracketed by CUDA
+ * events on its stream. qmckl_get_kernel_stats_device returns, for kernel slot `which`,
+ * its name, launch count and total milliseconds (completed work only). */
+qmckl_exit_code_device qmckl_set_profiling_device(qmckl_context_device context, int32_t enable);
+qmckl_exit_code_device qmckl_reset_kernel_stats_device(qmckl_context_device context);
+int32_t qmckl_get_kernel_stats_device(qmckl_context_device context, int32_t which, char* name, int64_t name_size,
+                                      int64_t* launches, double* total_ms);
+/* Total number of kernels the context has launched since creation or the last reset. */
+int64_t qmckl_get_launch_count_device(qmckl_context_device context);
+
+/* Test hook for allocation failure handling: the n-th device allocation from now on
+ * (n >= 1) fails as if cudaMalloc had failed; n = 0 disables the hook. */
+qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device context, int64_t n);
+
+/* Library build information: "sm_103a" plus the git-independent build flags. */
+const char* qmckl_gb300_build_info(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMCKL_GPU_H */

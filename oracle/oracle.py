@@ -1,0 +1,180 @@
+"""ctypes loader for the CPU oracle (qmckl_oracle.c) and, when it was built here, the
+unmodified reference library (oracle/_ref/libqmckl_ref.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the CPU
+baseline legs of bench.py, as the checker or the timed CPU baseline. The product
+(qmckl_sycl_gb300) never imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libqmckl_ref.so")
+REFERENCE_DIR = "/root/reference"
+
+_f64 = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_i64 = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_i32 = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+_I = ctypes.c_int64
+
+
+def build_oracle(force=False):
+    """Compiles qmckl_oracle.c (no FP contraction, OpenMP) into _build/liboracle.so."""
+    src = os.path.join(HERE, "qmckl_oracle.c")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+        return LIB_PATH
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+                           "-std=c11", src, "-o", tmp, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def build_reference(reference_dir=REFERENCE_DIR):
+    """Builds oracle/_ref/libqmckl_ref.so from the reference sources where they lie.
+    Returns the path, or None when the reference checkout is not present."""
+    if not os.path.isdir(os.path.join(reference_dir, "src")):
+        return None
+    subprocess.check_call(["make", "-s", "-j8", "-f", os.path.join(HERE, "Makefile.ref"),
+                           "REFERENCE=" + reference_dir], cwd=os.path.dirname(HERE))
+    return REF_PATH
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle()
+        L = ctypes.CDLL(LIB_PATH)
+        L.oracle_num_threads.restype = ctypes.c_int
+        L.oracle_set_num_threads.argtypes = [ctypes.c_int]
+        L.oracle_forward.restype = ctypes.c_int
+        L.oracle_forward.argtypes = [_I, _f64, _I, _I, _I, _i64, _i64, _i32, _i64, _i64, _f64, _f64, _f64, _f64,
+                                     _f64, _I, _f64, _I, _f64, _vp, _vp, _vp, _vp]
+        L.oracle_finalize_ao.argtypes = [_I, _I, _I, _i64, _i64, _i32, _i64, _i64, _f64, _f64, _f64, _f64,
+                                         _i64, _f64, _i32, _f64]
+        L.oracle_shell_vgl.argtypes = [_I, _I, _I, _i64, _i64, _f64, _i64, _i64, _f64, _f64, _f64, _f64, _f64]
+        L.oracle_mo_vgl.argtypes = [_I, _I, _I, _f64, _f64, _f64]
+        L.oracle_mo_value.argtypes = [_I, _I, _I, _f64, _f64, _f64]
+        _lib = L
+    return _lib
+
+
+def reference_lib():
+    """The unmodified reference built on the host, or None if unavailable."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PATH):
+            return None
+        L = ctypes.CDLL(REF_PATH)
+        argt = [_I, _f64, _f64, _I, _I, _I, _i64, _i64, _i32, _i64, _i64, _f64, _f64, _f64, _f64, _f64, _I,
+                _f64, _I, _f64]
+        L.ref_run.restype = ctypes.c_int
+        L.ref_run.argtypes = argt + [_vp, _vp, _vp, _vp]
+        L.ref_time_mo_vgl.restype = ctypes.c_int
+        L.ref_time_mo_vgl.argtypes = argt + [ctypes.c_int, _f64]
+        _ref = L
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _basis_args(s):
+    return (s.nucl_num, s.nucl_coord, s.shell_num, s.prim_num, s.ao_num, s.nucleus_index, s.nucleus_shell_num,
+            s.shell_ang_mom, s.shell_prim_num, s.shell_prim_index, s.shell_factor, s.exponent, s.coefficient,
+            s.prim_factor, s.ao_factor)
+
+
+def forward(s, coord_soa=None, want=("ao_vgl", "ao_value", "mo_vgl", "mo_value"), threads=0):
+    """Runs the oracle on a System `s` (see qmckl_sycl_gb300.synth). coord_soa is [3][P];
+    defaults to s.coord (which is [P][3]). Returns a dict of the requested arrays."""
+    L = lib()
+    if threads:
+        L.oracle_set_num_threads(int(threads))
+    if coord_soa is None:
+        coord_soa = np.ascontiguousarray(s.coord.T)
+    P = coord_soa.shape[1]
+    out = {}
+    if "ao_vgl" in want:
+        out["ao_vgl"] = np.zeros((P, 5, s.ao_num))
+    if "ao_value" in want:
+        out["ao_value"] = np.zeros((P, s.ao_num))
+    if "mo_vgl" in want:
+        out["mo_vgl"] = np.zeros((P, 5, s.mo_num))
+    if "mo_value" in want:
+        out["mo_value"] = np.zeros((P, s.mo_num))
+    rc = L.oracle_forward(*_basis_args(s), s.mo_num, s.mo_coef, P, np.ascontiguousarray(coord_soa),
+                          _ptr(out.get("ao_vgl")), _ptr(out.get("ao_value")), _ptr(out.get("mo_vgl")),
+                          _ptr(out.get("mo_value")))
+    assert rc == 0
+    return out
+
+
+def finalize(s):
+    L = lib()
+    npi = np.zeros(s.nucl_num + 1, np.int64)
+    cn = np.zeros(s.prim_num)
+    nmax = np.zeros(s.nucl_num, np.int32)
+    nr = np.zeros(s.nucl_num)
+    L.oracle_finalize_ao(s.nucl_num, s.shell_num, s.prim_num, s.nucleus_index, s.nucleus_shell_num,
+                         s.shell_ang_mom, s.shell_prim_index, s.shell_prim_num, s.exponent, s.coefficient,
+                         s.prim_factor, s.shell_factor, npi, cn, nmax, nr)
+    return dict(nucleus_prim_index=npi, coefficient_normalized=cn, nucleus_max_ang_mom=nmax, nucleus_range=nr)
+
+
+def shell_vgl(s, coord_soa=None):
+    L = lib()
+    fin = finalize(s)
+    if coord_soa is None:
+        coord_soa = np.ascontiguousarray(s.coord.T)
+    P = coord_soa.shape[1]
+    out = np.zeros((P, 5, s.shell_num))
+    L.oracle_shell_vgl(P, s.nucl_num, s.shell_num, s.nucleus_index, s.nucleus_shell_num, fin["nucleus_range"],
+                       s.shell_prim_index, s.shell_prim_num, np.ascontiguousarray(coord_soa), s.nucl_coord,
+                       s.exponent, fin["coefficient_normalized"], out)
+    return out
+
+
+def reference_forward(s, want=("ao_vgl", "ao_value", "mo_vgl", "mo_value")):
+    """Runs the unmodified reference (host build) through its own API; None if absent.
+    Points are passed as [P][3] with transp 'N', nuclei as [3][N] with 'T'."""
+    R = reference_lib()
+    if R is None:
+        return None
+    P = s.coord.shape[0]
+    out = {}
+    if "ao_vgl" in want:
+        out["ao_vgl"] = np.zeros((P, 5, s.ao_num))
+    if "ao_value" in want:
+        out["ao_value"] = np.zeros((P, s.ao_num))
+    if "mo_vgl" in want:
+        out["mo_vgl"] = np.zeros((P, 5, s.mo_num))
+    if "mo_value" in want:
+        out["mo_value"] = np.zeros((P, s.mo_num))
+    rc = R.ref_run(s.nucl_num, s.charge, *_basis_args(s)[1:], s.mo_num, s.mo_coef, P, np.ascontiguousarray(s.coord),
+                   _ptr(out.get("ao_vgl")), _ptr(out.get("ao_value")), _ptr(out.get("mo_vgl")),
+                   _ptr(out.get("mo_value")))
+    assert rc == 0, rc
+    return out
+
+
+def reference_time_mo_vgl(s, reps):
+    R = reference_lib()
+    if R is None:
+        return None
+    secs = np.zeros(reps)
+    rc = R.ref_time_mo_vgl(s.nucl_num, s.charge, *_basis_args(s)[1:], s.mo_num, s.mo_coef, s.coord.shape[0],
+                           np.ascontiguousarray(s.coord), reps, secs)
+    assert rc == 0, rc
+    return secs
