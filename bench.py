@@ -1,0 +1,406 @@
+"""Benchmark of the QMCkl basis-evaluation path on GB300: MO vgl points/s.
+
+A step is one evaluation of the hot path for one batch of points: touch the context (new
+point set) and provide mo_vgl = AO vgl (fused kernel) + MO contraction, for the medium
+workload (40 nuclei, 600 s/p/d/f shells -> 1188 AOs, 300 MOs, 256 walkers x 160 electrons
+= 40960 points; seeded synthetic data). `value` is measured with the inputs resident in
+HBM and timed with CUDA events on the library's stream; `e2e` is the same metric through
+the C ABI with host buffers (points copied in, mo_vgl copied out every step). The working
+set (ao_vgl 1.95 GB + mo_vgl 0.49 GB per step) is far larger than the 129 MB L2, so no L2
+flush is inserted between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--form fp64|mixed]
+
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU ("replicas
+only": the path has no exchange step); value = all points / max-over-ranks time.
+`--impl reference` times the reference algorithm on the host cores (the oracle port in
+oracle/, all threads) on the same workload and prints the same JSON line.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MO vgl points/sec on 1 GB300: mixed vs FP64 form at <=1e-6 rel err; % roofline"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--form", choices=["fp64", "mixed"], default=None)
+    p.add_argument("--walkers", type=int, default=256)
+    p.add_argument("--electrons", type=int, default=160)
+    p.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+class Dist:
+    """Rank bookkeeping; torch.distributed (gloo, CPU) only for the N > 1 barrier/max."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x):
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = max(smax, float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": FALLBACK_HBM_GBS}, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary
+    (profiles/ncu_traffic.txt, lines `kernel=<name> dram_bytes_per_point=<x>`)."""
+    out = {}
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if os.path.exists(path):
+        for line in open(path):
+            if line.startswith("kernel="):
+                kv = dict(t.split("=", 1) for t in line.split())
+                out[kv["kernel"]] = float(kv["dram_bytes_per_point"])
+    return out
+
+
+def cpu_baseline(s, seconds, threads=None):
+    """The reference algorithm (oracle port, all host threads) on samples of the same
+    workload until `seconds` of wall time: returns points/s and the sample description."""
+    from oracle import oracle
+
+    L = oracle.lib()
+    if threads:
+        L.oracle_set_num_threads(threads)
+    nthreads = L.oracle_num_threads()
+    n = min(s.point_num, max(256, 64 * nthreads))
+    rng = np.random.default_rng(7)
+    done, t_total, reps = 0, 0.0, 0
+    while t_total < seconds and reps < 50:
+        idx = rng.choice(s.point_num, size=n, replace=False)
+        sub = s.with_points(s.coord[np.sort(idx)])
+        t0 = time.perf_counter()
+        oracle.forward(sub, want=("mo_vgl",))
+        t_total += time.perf_counter() - t0
+        done += n
+        reps += 1
+    return done / t_total, nthreads, "%d samples x %d points of the workload, %.1f s wall" % (reps, n, t_total)
+
+
+def run_reference(args, dist):
+    from qmckl_sycl_gb300.systems import config_medium
+
+    if dist.rank != 0:
+        return
+    s = config_medium(0, args.walkers, args.electrons)
+    from oracle import oracle
+
+    nthreads = oracle.lib().oracle_num_threads()
+    times = []
+    n = min(s.point_num, max(256, 64 * nthreads))
+    rng = np.random.default_rng(11)
+    for i in range(args.warmup + args.steps):
+        sub = s.with_points(s.coord[np.sort(rng.choice(s.point_num, size=n, replace=False))])
+        t0 = time.perf_counter()
+        oracle.forward(sub, want=("mo_vgl",))
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    v = n * len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(s, "reference CPU path (oracle port of src/qmckl_ao_sycl.cpp + src/qmckl_mo_sycl.cpp)"),
+        "cpu_baseline": {"value": v, "unit": "points/s", "cores": nthreads, "kind": "port",
+                         "sample": "%d random points of the workload per step" % n},
+        "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(s, form):
+    return {"workload": "medium: %d nuclei, %d shells, %d primitives, %d AOs, %d MOs, %d points (%s)" % (
+        s.nucl_num, s.shell_num, s.prim_num, s.ao_num, s.mo_num, s.point_num, form),
+            "nucl_num": s.nucl_num, "shell_num": s.shell_num, "prim_num": s.prim_num, "ao_num": s.ao_num,
+            "mo_num": s.mo_num, "point_num": s.point_num, "seed": 0,
+            "l2": "no flush: per-step working set %.2f GB (ao_vgl + mo_vgl) > 129 MB L2" % (
+                8.0 * 5 * s.point_num * (s.ao_num + s.mo_num) / 1e9)}
+
+
+def time_form(ctx, s, form, steps, warmup, dist, clocks=None):
+    from qmckl_sycl_gb300 import PRECISION_FP64, PRECISION_SPLIT_BF16
+
+    ctx.set_precision(PRECISION_FP64 if form == "fp64" else PRECISION_SPLIT_BF16)
+    ctx.set_async(True)
+    for _ in range(warmup):
+        ctx.touch()
+        ctx.call("provide_mo_basis_mo_vgl")
+    ctx.synchronize()
+    ctx.reset_kernel_stats()
+    dist.barrier()
+    ctx.synchronize()
+    sampler = clocks or _NullCtx()
+    with sampler:
+        ctx.call("timer_start")
+        for _ in range(steps):
+            ctx.touch()
+            ctx.call("provide_mo_basis_mo_vgl")
+        ms = ctypes.c_double(0)
+        ctx.call("timer_stop", ctypes.byref(ms))
+    ctx.synchronize()
+    stats = ctx.kernel_stats()
+    launches = ctx.launch_count()
+    ctx.set_async(False)
+    return ms.value, stats, launches
+
+
+class _NullCtx:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def time_e2e(ctx, s, steps, warmup):
+    """Through the C ABI with host buffers: page-locked coordinates in, mo_vgl out."""
+    L = ctx.L
+    P, M = s.point_num, s.mo_num
+    coord = np.ascontiguousarray(s.coord)
+    out = np.empty((P, 5, M))
+    ctx.call("host_register", coord.ctypes.data_as(ctypes.c_void_p), coord.nbytes)
+    ctx.call("host_register", out.ctypes.data_as(ctypes.c_void_p), out.nbytes)
+    cptr = coord.ctypes.data_as(ctypes.c_void_p)
+    optr = out.ctypes.data_as(ctypes.c_void_p)
+    try:
+        for i in range(warmup + steps):
+            if i == warmup:
+                t0 = time.perf_counter()
+            ctx.call("set_point", b"N", P, cptr, 3 * P)
+            ctx.call("get_mo_basis_mo_vgl", optr, out.size)
+        dt = time.perf_counter() - t0
+    finally:
+        ctx.call("host_unregister", coord.ctypes.data_as(ctypes.c_void_p))
+        ctx.call("host_unregister", out.ctypes.data_as(ctypes.c_void_p))
+    return dt, coord.nbytes, out.nbytes, out
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+        return
+    from qmckl_sycl_gb300 import Context, config_medium
+
+    s = config_medium(0, args.walkers, args.electrons)
+    P, A, M = s.point_num, s.ao_num, s.mo_num
+    ctx = Context(dist.local_rank)
+    ctx.set_profiling(True)
+    ctx.load_system(s)
+    fp64_peak = ctypes.c_double(0)
+    ctx.call("measure_fp64_peak", ctypes.byref(fp64_peak))
+    peaks, peak_src = measured_peaks()
+    traffic = ncu_traffic()
+
+    forms = ["fp64"]
+    try:
+        ctx.set_precision(1)
+        ctx.touch()
+        ctx.call("provide_mo_basis_mo_vgl")
+        forms.append("mixed")
+    except Exception:
+        pass
+    ctx.set_precision(0)
+    headline = args.form or ("mixed" if "mixed" in forms else "fp64")
+
+    results = {}
+    clocks = ClockSampler(dist.local_rank)
+    for form in forms:
+        ms, stats, launches = time_form(ctx, s, form, args.steps, args.warmup, dist,
+                                        clocks if form == headline else None)
+        t = dist.max(ms)
+        total_points = dist.sum(P * args.steps)
+        results[form] = dict(ms=t, value=total_points / (t * 1e-3), stats=stats, launches=launches)
+
+    # accuracy of the mixed form against the FP64 form on the same inputs
+    acc = None
+    if "mixed" in forms:
+        ctx.set_precision(0)
+        ctx.touch()
+        ref = ctx.get_mo_vgl(P)
+        ctx.set_precision(1)
+        ctx.touch()
+        got = ctx.get_mo_vgl(P)
+        scale = np.abs(ref).max(axis=(0, 2))
+        acc = {"max_abs": [float(x) for x in np.abs(got - ref).max(axis=(0, 2))],
+               "max_rel_normwise": [float(x) for x in np.abs(got - ref).max(axis=(0, 2)) / scale]}
+        del ref, got
+
+    # end to end through the C ABI with host buffers (headline form)
+    ctx.set_precision(0 if headline == "fp64" else 1)
+    e2e_dt, h2d, d2h, _ = time_e2e(ctx, s, args.steps, min(args.warmup, 2))
+    e2e_dt = dist.max(e2e_dt)
+    e2e_value = dist.sum(P * args.steps) / e2e_dt
+
+    def roof(form):
+        st = results[form]["stats"]
+        out = {}
+        if "ao_vgl_fused" in st:
+            n, tot = st["ao_vgl_fused"]
+            ms = tot / max(n, 1)
+            alg = 8.0 * (5 * A + 3) * P
+            out["ao_vgl_fused"] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9,
+                                   "peak": peaks["hbm_gbs"], "unit": "GB/s", "ms_per_launch": ms,
+                                   "traffic": traffic.get("ao_vgl_fused", 0) * P or None}
+            out["ao_vgl_fused"]["frac"] = out["ao_vgl_fused"]["achieved"] / peaks["hbm_gbs"]
+        for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
+            if k in st:
+                n, tot = st[k]
+                ms = tot / max(n, 1)
+                flops = 10.0 * A * M * P
+                pk = fp64_peak.value if k == "mo_vgl_dgemm" else peaks.get("bf16_tflops", 1909.5)
+                out[k] = {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12, "peak": pk, "unit": "TFLOP/s",
+                          "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
+                out[k]["frac"] = out[k]["achieved"] / pk
+        return out
+
+    rf = {f: roof(f) for f in forms}
+    head = rf[headline]
+    dom = max(head, key=lambda k: head[k]["ms_per_launch"])
+    roofline = dict(head[dom])
+    roofline["kernel"] = dom
+    roofline["peak_source"] = ("live DMMA m16n8k4 f64 probe (MEASURED_PEAKS.json has no FP64 figure)"
+                               if dom == "mo_vgl_dgemm" else "%s MEASURED_PEAKS.json" % peak_src)
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_baseline(s, args.cpu_seconds)
+        cpu = {"value": v, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample}
+
+    if dist.rank != 0:
+        return
+    hr = results[headline]
+    line = {
+        "metric": METRIC, "value": hr["value"], "unit": "points/s", "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": hr["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if headline == "fp64" else "f64+bf16x3",
+        "data": "synthetic (seeded generator with the medium configuration's shapes and distributions)",
+        "config": config_dict(s, "%s form" % headline),
+        "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": hr["launches"], "clocks": clocks.summary(),
+        "forms": {f: {"value": results[f]["value"], "ms_per_step": results[f]["ms"] / args.steps,
+                      "kernels": rf[f]} for f in forms},
+        "fp64_peak_tflops": fp64_peak.value,
+    }
+    if acc:
+        line["mixed_vs_fp64_error"] = acc
+        line["mixed_over_fp64"] = results["mixed"]["value"] / results["fp64"]["value"]
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -305,6 +305,21 @@ int32_t qmckl_get_kernel_stats_device(qmckl_context_device context, int32_t whic
 /* Total number of kernels the context has launched since creation or the last reset. */
 int64_t qmckl_get_launch_count_device(qmckl_context_device context);
 
+/* Device-side timing of the work issued on the context's stream: start records a CUDA
+ * event on the stream; stop records a second one, waits for it and returns the elapsed
+ * milliseconds. */
+qmckl_exit_code_device qmckl_timer_start_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_timer_stop_device(qmckl_context_device context, double* elapsed_ms);
+
+/* Page-locks (or releases) a caller's host buffer so that transfers to and from it run
+ * at full link speed and kernels may read it directly. */
+qmckl_exit_code_device qmckl_host_register_device(qmckl_context_device context, void* ptr, size_t size);
+qmckl_exit_code_device qmckl_host_unregister_device(qmckl_context_device context, void* ptr);
+
+/* Measures the FP64 tensor-pipe (DMMA) throughput of the context's GPU in TFLOP/s with a
+ * register-resident mma loop over every SM (a roofline denominator for the FP64 form). */
+qmckl_exit_code_device qmckl_measure_fp64_peak_device(qmckl_context_device context, double* tflops);
+
 /* Test hook for allocation failure handling: the n-th device allocation from now on
  * (n >= 1) fails as if cudaMalloc had failed; n = 0 disables the hook. */
 qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device context, int64_t n);

@@ -1,0 +1,267 @@
+// Internal definitions of the GB300 QMCkl basis-evaluation library: the context
+// structure, the packed device tables the fused kernels read, and the launch
+// interfaces of the CUDA kernels. Not part of the public ABI (include/qmckl_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/qmckl_gpu.h"
+
+namespace qg {
+
+constexpr uint64_t kValidTag = 0xBEEFFACEull;    // include/qmckl_types.hpp:12 of the reference
+constexpr uint64_t kInvalidTag = 0xDEADBEEFull;  // include/qmckl_types.hpp:13
+// -ln(1e-12): screening cutoff hard-coded by the reference (src/qmckl_ao_sycl.cpp:22,117,449).
+constexpr double kCutoff = 27.631021115928547;
+// Largest angular momentum handled; the reference's lstart table has 21 entries
+// (src/qmckl_ao_sycl.cpp:161), i.e. l + 1 <= 20.
+constexpr int kMaxL = 19;
+
+// ---- Packed tables read by the fused AO kernels (built on the host at finalize) ----
+// Nuclei are visited in index order and, within a nucleus, its shells in index order;
+// this is the order in which the reference numbers AOs (src/qmckl_ao_sycl.cpp:166-188).
+struct NucleusEntry {      // 64 bytes
+  double x, y, z;          // nucleus coordinates
+  uint64_t screen_bits;    // bit pattern of fl(cutoff * nucleus_range): a point is screened for
+                           // this nucleus iff bits(r2) > screen_bits (non-negative doubles order
+                           // like their bit patterns), the reference's test at ao_sycl.cpp:53
+  int32_t shell_begin, shell_end;  // range in the packed shell list
+  int32_t ao_begin, ao_end;        // AO columns of this nucleus
+  int32_t lmax, pad;
+};
+struct ShellEntry {        // 16 bytes
+  int32_t prim_begin, prim_end;  // range in the packed primitive list
+  int32_t ao_begin;
+  int16_t l;
+  int16_t orig;            // unused (the original index lives in shell_orig)
+};
+struct PrimEntry {         // 32 bytes
+  double expo;
+  double coef;             // coefficient_normalized = coefficient * prim_factor * shell_factor
+  double m2a;              // -2 * expo (exact)
+  uint64_t thr_bits;       // bits of the smallest r2 with fl(expo * r2) > cutoff: the primitive
+                           // is skipped iff bits(r2) >= thr_bits (ao_sycl.cpp:72-75)
+};
+
+// A contiguous group of nuclei processed by one warp task.
+struct NucleusChunk {
+  int32_t nucl_begin, nucl_end;
+  int32_t ao_begin, ao_end;
+};
+
+struct AoTables {
+  NucleusEntry* nuclei = nullptr;   // [nucl_num]
+  ShellEntry* shells = nullptr;     // [shell_num] packed
+  PrimEntry* prims = nullptr;       // [prim_num] packed
+  double* ao_factor = nullptr;      // [ao_num]
+  int32_t* shell_orig = nullptr;    // packed shell -> user shell index
+  int32_t* shell_nucl = nullptr;    // packed shell -> nucleus
+  NucleusChunk* chunks = nullptr;   // all chunk levels, concatenated
+  // Level v splits the nuclei into level_sizes[v] chunks of balanced cost, stored at
+  // chunks + level_offsets[v]; the launch picks the level that fills the GPU.
+  std::vector<int32_t> level_offsets, level_sizes;
+  int32_t nucl_num = 0, shell_num = 0, prim_num = 0, ao_num = 0, lmax = 0;
+  int sm_count = 152;
+  bool valid = false;
+  std::vector<NucleusEntry> h_nuclei;
+  std::vector<ShellEntry> h_shells;
+  std::vector<PrimEntry> h_prims;
+  std::vector<NucleusChunk> h_chunks;
+  std::vector<int32_t> h_shell_orig, h_shell_nucl;
+  std::vector<double> h_ao_factor;
+};
+
+struct PointData {
+  int64_t num = 0;
+  uint64_t date = 0;
+  double* coord = nullptr;  // [3][num] (the reference's ctx->point.coord, Fortran (num,3))
+};
+
+struct WalkerData {
+  int64_t num = 0;
+  PointData point;
+};
+
+struct ElectronData {
+  int64_t num = 0, up_num = 0, down_num = 0;
+  WalkerData walker, walker_old;
+  int32_t uninitialized = 0;
+  bool provided = false;
+};
+
+struct NucleusData {
+  int64_t num = 0;
+  double* charge = nullptr;  // [num]
+  double* coord = nullptr;   // [3][num]
+  int32_t uninitialized = 0;
+  bool provided = false;
+};
+
+struct AoBasisData {
+  char type = 0;
+  int64_t shell_num = 0, prim_num = 0, ao_num = 0;
+  int64_t* nucleus_index = nullptr;
+  int64_t* nucleus_shell_num = nullptr;
+  int32_t* shell_ang_mom = nullptr;
+  int64_t* shell_prim_num = nullptr;
+  int64_t* shell_prim_index = nullptr;
+  double* shell_factor = nullptr;
+  double* exponent = nullptr;
+  double* coefficient = nullptr;
+  double* prim_factor = nullptr;
+  double* ao_factor = nullptr;
+  // derived at finalize (src/qmckl_ao_sycl.cpp:1087-1231)
+  int64_t* nucleus_prim_index = nullptr;
+  double* coefficient_normalized = nullptr;
+  int32_t* nucleus_max_ang_mom = nullptr;
+  double* nucleus_range = nullptr;
+  AoTables tables;
+  // caches
+  double* shell_vgl = nullptr;
+  size_t shell_vgl_cap = 0;
+  uint64_t shell_vgl_date = 0;
+  double* ao_vgl = nullptr;
+  size_t ao_vgl_cap = 0;
+  uint64_t ao_vgl_date = 0;
+  double* ao_value = nullptr;
+  size_t ao_value_cap = 0;
+  uint64_t ao_value_date = 0;
+  int32_t uninitialized = 0;
+  bool provided = false;
+};
+
+struct MoBasisData {
+  int64_t mo_num = 0;
+  double* coefficient = nullptr;    // [mo_num][ao_num]
+  double* coefficient_t = nullptr;  // [ao_num][mo_num]
+  double* mo_vgl = nullptr;
+  size_t mo_vgl_cap = 0;
+  uint64_t mo_vgl_date = 0;
+  double* mo_value = nullptr;
+  size_t mo_value_cap = 0;
+  uint64_t mo_value_date = 0;
+  // split-BF16 form: the coefficient split into three BF16 planes (hi, mid, lo), each
+  // [mo_pad][ao_pad] K-major, and the AO operand planes for the current points.
+  void* coef_split = nullptr;
+  int64_t split_mo_pad = 0, split_ao_pad = 0;
+  void* ao_split = nullptr;
+  size_t ao_split_cap = 0;
+  int32_t uninitialized = 0;
+  bool provided = false;
+};
+
+struct KernelStat {
+  std::string name;
+  int64_t launches = 0;
+  double total_ms = 0.0;
+};
+struct PendingEvent {
+  int slot;
+  cudaEvent_t start, stop;
+};
+
+}  // namespace qg
+
+struct qmckl_error_struct_device {
+  qmckl_exit_code_device exit_code = 0;
+  char function[QMCKL_MAX_FUN_LEN_DEVICE] = {0};
+  char message[QMCKL_MAX_MSG_LEN_DEVICE] = {0};
+};
+
+struct qmckl_context_struct_device {
+  uint64_t tag = qg::kValidTag;
+  int32_t device_id = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  bool async = false;
+  int32_t precision = QMCKL_PRECISION_FP64_DEVICE;
+
+  std::recursive_mutex mutex;
+  int lock_count = 0;
+  qmckl_error_struct_device error;
+
+  // allocation registries (src/qmckl_memory.cpp:15-220 of the reference)
+  std::unordered_map<void*, size_t> device_allocs;
+  std::unordered_map<void*, size_t> host_allocs;
+  int64_t fail_alloc_countdown = 0;
+
+  uint64_t date = 0;
+  qg::PointData point;
+  qg::NucleusData nucleus;
+  qg::ElectronData electron;
+  qg::AoBasisData ao_basis;
+  qg::MoBasisData mo_basis;
+
+  // grow-only scratch for layout changes of host inputs (points, nuclei)
+  void* staging = nullptr;
+  size_t staging_cap = 0;
+
+  // profiling
+  bool profiling = false;
+  std::vector<qg::KernelStat> stats;
+  std::vector<qg::PendingEvent> pending;
+  std::vector<cudaEvent_t> event_pool;
+  int64_t launch_count = 0;
+};
+
+namespace qg {
+
+using Ctx = qmckl_context_struct_device;
+
+inline Ctx* ctx_of(qmckl_context_device c) { return reinterpret_cast<Ctx*>(c); }
+
+// Error helpers (record in ctx->error like qmckl_failwith_device).
+qmckl_exit_code_device fail(qmckl_context_device c, qmckl_exit_code_device code, const char* fn, const char* msg);
+
+// Device memory owned by the context (registered, freed at destroy).
+void* dalloc(Ctx* ctx, size_t bytes);
+void dfree(Ctx* ctx, void* p);
+// Ensures *buf holds at least `bytes`, reallocating (contents not kept) when smaller.
+bool ensure(Ctx* ctx, double** buf, size_t* cap, size_t bytes);
+bool ensure_raw(Ctx* ctx, void** buf, size_t* cap, size_t bytes);
+
+// Selects the context's device and creates its stream on first use.
+bool ensure_device(Ctx* ctx);
+// True when a kernel may dereference p (device, managed or page-locked host memory).
+bool gpu_accessible(const void* p);
+// The context's grow-only staging buffer, at least `bytes` long (nullptr on failure).
+void* staging(Ctx* ctx, size_t bytes);
+
+// Synchronous unless ctx->async.
+qmckl_exit_code_device finish(Ctx* ctx, qmckl_context_device c, const char* fn);
+qmckl_exit_code_device copy(Ctx* ctx, qmckl_context_device c, void* dst, const void* src, size_t bytes,
+                            const char* fn, bool force_sync = false);
+
+// Kernel launch bracketing for profiling; slot names are stable strings.
+struct LaunchScope {
+  Ctx* ctx;
+  int slot;
+  cudaEvent_t start = nullptr, stop = nullptr;
+  LaunchScope(Ctx* c, const char* name);
+  ~LaunchScope();
+};
+
+// ---- kernel entry points (ao_kernels.cu, mo_kernels.cu, util_kernels.cu) ----
+cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* ao_vgl);
+cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* ao_value);
+cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num,
+                             int64_t shell_num, double* shell_vgl);
+// mo_vgl[5P][M] = ao_vgl[5P][A] * coef_t[A][M], skipping (for components 1..4) the AOs whose
+// value is exactly zero, as the reference does (src/qmckl_mo_sycl.cpp:40).
+cudaError_t launch_mo_vgl_fp64(Ctx* ctx, const double* ao_vgl, const double* coef_t, int64_t point_num,
+                               int64_t ao_num, int64_t mo_num, double* mo_vgl);
+cudaError_t launch_mo_value_fp64(Ctx* ctx, const double* ao_value, const double* coef_t, int64_t point_num,
+                                 int64_t ao_num, int64_t mo_num, double* mo_value);
+cudaError_t launch_transpose(Ctx* ctx, const double* in, int64_t rows, int64_t cols, double* out);
+cudaError_t launch_strided_copy(Ctx* ctx, const double* in, int64_t in_stride, double* out, int64_t out_stride,
+                                int64_t rows, int64_t cols);
+cudaError_t launch_fill(Ctx* ctx, double* p, int64_t n, double v);
+cudaError_t launch_point_aos_to_soa(Ctx* ctx, const double* in, int64_t num, double* out);
+
+}  // namespace qg

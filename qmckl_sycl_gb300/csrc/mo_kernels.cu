@@ -1,0 +1,124 @@
+// FP64 MO contraction on the FP64 tensor pipe (DMMA, mma.sync m16n8k4 .f64) for sm_103a.
+//
+//   mo_vgl[5P][M] = ao_vgl[5P][A] * coef_t[A][M]        (rows r = 5*point + component)
+//   mo_value[P][M] = ao_value[P][A] * coef_t[A][M]
+//
+// Reference: src/qmckl_mo_sycl.cpp:24-50 (one work-item per point, serial triple loop) and
+// :77-129 (value only). The reference skips AO k of a point, for every component, when that
+// AO's *value* is exactly zero (:40). For the value row the skip changes nothing; for the
+// gradient and Laplacian rows it drops the term, so this kernel applies the same mask: an
+// element (5p + c, k) with c > 0 is read as zero when ao_vgl[5p][k] == 0.
+//
+// On GB300 the FP64 pipe (DFMA and DMMA alike) delivers ~1.05 TFLOP/s, so this GEMM is
+// bound by DMMA issue, with arithmetic intensity ~2M/(8(1+M/A)) FLOP/byte: no shared-memory
+// staging is needed to feed it. Each warp owns a 32x32 output tile (2 x 4 m16n8 fragments)
+// and reads its A and B fragments straight from L1/L2; a CTA of 4 warps covers 64 rows x
+// 64 columns so that neighbouring warps share A rows in L1.
+#include <cstdint>
+
+#include "internal.hpp"
+
+namespace qg {
+namespace {
+
+constexpr int kWM = 32, kWN = 32;     // warp tile
+constexpr int kCM = 64, kCN = 64;     // CTA tile (2 x 2 warps)
+
+__device__ __forceinline__ void dmma_16x8x4(double (&d)[4], double a0, double a1, double b0) {
+  asm volatile("mma.sync.aligned.m16n8k4.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};\n"
+               : "+d"(d[0]), "+d"(d[1]), "+d"(d[2]), "+d"(d[3])
+               : "d"(a0), "d"(a1), "d"(b0));
+}
+
+// Element (r, k) of A (row-major, ld = K) with bounds and, when MASK, the reference's
+// zero-value skip for rows whose component (r % 5) is not 0.
+template <bool MASK>
+__device__ __forceinline__ double load_a(const double* __restrict__ A, int64_t R, int64_t K, int64_t r, int64_t k) {
+  if (r >= R || k >= K) return 0.0;
+  double v = __ldg(A + r * K + k);
+  if constexpr (MASK) {
+    const int comp = (int)(r % 5);
+    if (comp != 0) {
+      const double v0 = __ldg(A + (r - comp) * K + k);
+      if (v0 == 0.0) v = 0.0;
+    }
+  }
+  return v;
+}
+
+template <bool MASK>
+__global__ void __launch_bounds__(128) dgemm_dmma_kernel(const double* __restrict__ A, const double* __restrict__ B,
+                                                         double* __restrict__ C, int64_t R, int64_t K, int64_t N) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
+  const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
+  if (r0 >= R || c0 >= N) return;  // warp-uniform
+  double acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.0;
+
+  bool colok[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) colok[j] = c0 + 8 * j + g < N;
+
+#pragma unroll 2
+  for (int64_t k = 0; k < K; k += 4) {
+    double a[2][2], b[4];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      a[i][0] = load_a<MASK>(A, R, K, r0 + 16 * i + g, k + t);
+      a[i][1] = load_a<MASK>(A, R, K, r0 + 16 * i + g + 8, k + t);
+    }
+    const bool kok = k + t < K;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) b[j] = (kok && colok[j]) ? __ldg(B + (k + t) * N + c0 + 8 * j + g) : 0.0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dmma_16x8x4(acc[i][j], a[i][0], a[i][1], b[j]);
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t col = c0 + 8 * j + 2 * t;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int64_t row = r0 + 16 * i + g + 8 * h;
+        if (row < R) {
+          if (col < N) C[row * N + col] = acc[i][j][2 * h];
+          if (col + 1 < N) C[row * N + col + 1] = acc[i][j][2 * h + 1];
+        }
+      }
+    }
+}
+
+template <bool MASK>
+cudaError_t launch_dgemm(Ctx* ctx, const double* A, const double* B, double* C, int64_t R, int64_t K, int64_t N,
+                         const char* name) {
+  if (R <= 0 || N <= 0) return cudaSuccess;
+  if (K <= 0) return cudaMemsetAsync(C, 0, sizeof(double) * R * N, ctx->stream);
+  dim3 grid((unsigned)((N + kCN - 1) / kCN), (unsigned)((R + kCM - 1) / kCM));
+  LaunchScope scope(ctx, name);
+  dgemm_dmma_kernel<MASK><<<grid, 128, 0, ctx->stream>>>(A, B, C, R, K, N);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_mo_vgl_fp64(Ctx* ctx, const double* ao_vgl, const double* coef_t, int64_t point_num,
+                               int64_t ao_num, int64_t mo_num, double* mo_vgl) {
+  return launch_dgemm<true>(ctx, ao_vgl, coef_t, mo_vgl, 5 * point_num, ao_num, mo_num, "mo_vgl_dgemm");
+}
+
+cudaError_t launch_mo_value_fp64(Ctx* ctx, const double* ao_value, const double* coef_t, int64_t point_num,
+                                 int64_t ao_num, int64_t mo_num, double* mo_value) {
+  return launch_dgemm<false>(ctx, ao_value, coef_t, mo_value, point_num, ao_num, mo_num, "mo_value_dgemm");
+}
+
+}  // namespace qg

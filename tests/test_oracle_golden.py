@@ -1,0 +1,63 @@
+"""Pins the CPU oracle (oracle/qmckl_oracle.c) before it is trusted as the checker:
+against the reference's own golden file and known answers, and bit for bit against the
+unmodified reference built on this host (when the reference checkout is present)."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from qmckl_sycl_gb300.systems import config_adjoint, config_medium, config_small
+
+
+def test_oracle_matches_golden_mo_vgl(chbrclf, golden):
+    # tests/test_qmckl_mo.cpp:382-405 of the reference: every mo_vgl value at 1e-14 absolute
+    out = oracle.forward(chbrclf, want=("mo_vgl",))
+    ref = golden["mo_vgl_ref"]
+    assert out["mo_vgl"].shape == ref.shape
+    assert np.abs(out["mo_vgl"] - ref).max() <= 1e-14
+
+
+def test_oracle_known_answers(chbrclf, golden):
+    # ao_value[26][219..222] on walker 0 (tests/test_qmckl_ao.cpp:440-448)
+    s0 = chbrclf.with_points(chbrclf.coord[:68])
+    out = oracle.forward(s0, want=("ao_value",))
+    for p, a, v in golden["kat_ao_value"]:
+        assert abs(out["ao_value"][int(p), int(a)] - v) <= float(golden["kat_ao_value_tol"])
+    # ao_vgl[26][0..4][219] on both walkers (tests/test_qmckl_mo.cpp:250-259)
+    out = oracle.forward(chbrclf, want=("ao_vgl",))
+    for p, c, a, v in golden["kat_ao_vgl"]:
+        assert abs(out["ao_vgl"][int(p), int(c), int(a)] - v) <= float(golden["kat_ao_vgl_tol"])
+
+
+def test_oracle_mo_value_consistent_with_mo_vgl(chbrclf):
+    # tests/test_qmckl_mo.cpp:301-356: mo_value == mo_vgl[:, 0, :] within 1e-12
+    out = oracle.forward(chbrclf, want=("mo_vgl", "mo_value"))
+    assert np.abs(out["mo_value"] - out["mo_vgl"][:, 0, :]).max() <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium64"])
+def test_oracle_bitwise_equal_to_reference(name, chbrclf):
+    if oracle.reference_lib() is None:
+        pytest.skip("reference library not built on this machine (needs the reference checkout)")
+    s = {"chbrclf": lambda: chbrclf, "small": lambda: config_small(0), "adjoint": lambda: config_adjoint(0),
+         "medium64": lambda: config_medium(0, walkers=1, electrons=64)}[name]()
+    want = ("ao_vgl", "ao_value", "mo_vgl", "mo_value")
+    r = oracle.reference_forward(s, want=want)
+    o = oracle.forward(s, want=want)
+    for k in want:
+        assert np.array_equal(r[k], o[k]), k
+
+
+def test_oracle_shell_vgl_matches_reference_layout(chbrclf):
+    sv = oracle.shell_vgl(chbrclf)
+    assert sv.shape == (chbrclf.point_num, 5, chbrclf.shell_num)
+    # s shells contribute their radial value directly to their AO value (ao_factor 1)
+    ao = oracle.forward(chbrclf, want=("ao_vgl",))["ao_vgl"]
+    assert np.array_equal(sv[:, 0, 0] * chbrclf.ao_factor[0], ao[:, 0, 0])
+
+
+def test_oracle_threads_do_not_change_bits():
+    s = config_small(3, point_num=200)
+    a = oracle.forward(s, threads=1)
+    b = oracle.forward(s, threads=4)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
