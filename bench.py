@@ -347,7 +347,7 @@ def main():
     def roof(form):
         st = results[form]["stats"]
         out = {}
-        if "ao_vgl_fused" in st:
+        if st.get("ao_vgl_fused", (0, 0))[0] > 0:
             n, tot = st["ao_vgl_fused"]
             ms = tot / max(n, 1)
             alg = 8.0 * (5 * A + 3) * P
@@ -356,7 +356,7 @@ def main():
                                    "traffic": traffic.get("ao_vgl_fused", 0) * P or None}
             out["ao_vgl_fused"]["frac"] = out["ao_vgl_fused"]["achieved"] / peaks["hbm_gbs"]
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
-            if k in st:
+            if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]
                 ms = tot / max(n, 1)
                 flops = 10.0 * A * M * P

@@ -1,13 +1,518 @@
-// Split-BF16 MO contraction on the tcgen05 tensor cores (precision form).
+// Split-BF16 MO contraction on the tcgen05 tensor cores (the precision form).
+//
+//   mo[r][m] = sum_k ao[r][k] * coef[m][k],   r = 5*point + component (or point, value only)
+//
+// Each FP64 operand x is split into three BF16 terms x ~ x_hi + x_mid + x_lo (24 significant
+// bits), and the product is formed from the six terms whose order is above 2^-24:
+//   hi*hi + hi*mid + mid*hi + hi*lo + mid*mid + lo*hi
+// on tcgen05.mma kind::f16 (BF16 x BF16 -> FP32 in tensor memory). Distances, exponentials,
+// screening and the AO Laplacian assembly stay FP64 (the AO kernel); only this contraction
+// runs on the BF16 tensor cores. The reference computes it in FP64 with one work-item per
+// point (src/qmckl_mo_sycl.cpp:24-50); the AO-value-is-zero skip of its line 40 is applied
+// when the AO operand is split.
+//
+// The split avoids the FP64 pipe entirely (on GB300 it issues at ~1/66 of the FP32 rate):
+// the double is rounded to float with integer instructions on its bit pattern, and the
+// three BF16 terms are peeled off in FP32, where every subtraction is exact.
+//
+// Accumulation. The tensor core adds each MMA's products into the FP32 accumulator with a
+// truncating alignment, so every MMA costs an error of order 2^-24 of the accumulator (and of
+// its largest product). The five correction products (all ~2^-8 of the result or smaller)
+// go into their own accumulator; the main hi*hi product is accumulated for one 64-wide K
+// block at a time (four MMAs) in one of two ping-pong buffers, and the epilogue warps fold
+// each finished block into a running FP32 two-sum (hi, lo) kept in tensor memory while the
+// next block is multiplied. The error therefore does not grow with K. The FP64 result is
+// hi + lo + corrections, formed with a single FP64 addition.
+//
+// GEMM structure (one 128 x N output tile per CTA, N <= 96): warp 0 issues TMA loads of the
+// six operand planes per 64-wide K block into a two-stage ring of 128B-swizzled shared
+// memory buffers; warp 1 owns tensor memory and issues the MMAs (24 per K block: six
+// products x four K=16 steps); warps 2-5 (each its 32-lane quarter of tensor memory) fold
+// the main product per block and finally store the FP64 results. Every mbarrier wait
+// is bounded (~1 s); on expiry the kernel records an error code, drains what it issued,
+// releases its tensor memory and exits, and the host reports QMCKL_FAILURE_DEVICE.
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
 #include "internal.hpp"
 
 namespace qg {
+namespace {
+
+constexpr int kBM = 128;        // rows per tile (UMMA M)
+constexpr int kBK = 64;         // K per stage: 64 BF16 = 128 bytes = one swizzle row
+constexpr int kStages = 2;
+constexpr int kMaxN = 96;       // columns per tile: 5 * N <= 512 TMEM columns
+constexpr int kThreads = 192;   // 6 warps
+constexpr uint32_t kPlaneA = kBM * kBK * 2;  // 16 KB per A plane and stage
+constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
+
+// ------------------------------------------------------------------ split helpers
+// Double -> float, round to nearest even, by integer operations on the bit pattern (no FP64
+// instruction). Values below the float normal range flush to a signed zero; AO and MO
+// coefficients are far inside the float range.
+__device__ __forceinline__ float f64_to_f32_int(double a) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  if (e <= 0) return __uint_as_float(sign);
+  if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+  const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+  unsigned int m = (unsigned int)(frac >> 29);
+  const unsigned long long rem = frac & 0x1FFFFFFFull;
+  unsigned int bits = ((unsigned int)e << 23) | m;
+  if (rem > 0x10000000ull || (rem == 0x10000000ull && (m & 1u))) bits += 1u;  // carry may bump the exponent
+  return __uint_as_float(sign | bits);
+}
+
+// Float -> double exactly, by integer operations for normal numbers and zero.
+__device__ __forceinline__ double f32_to_f64_int(float f) {
+  const unsigned int u = __float_as_uint(f);
+  const unsigned int e = (u >> 23) & 0xFF;
+  if (e == 0 || e == 0xFF) return (double)f;  // zero, subnormal, inf, nan (rare)
+  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)(e + 896) << 52) |
+                                  ((unsigned long long)(u & 0x7FFFFF) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ void split3(double a, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
+  const float f = f64_to_f32_int(a);
+  hi = __float2bfloat16_rn(f);
+  const float r1 = f - __bfloat162float(hi);
+  mid = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(mid);
+  lo = __float2bfloat16_rn(r2);
+}
+
+// src [rows][ld_src] FP64 -> planes [3][rows][kp] BF16, zero in columns [k, kp). With
+// mask5, an element of a row whose component (row % 5) is not 0 is zeroed when the value
+// row of the same point has a zero in that column (src/qmckl_mo_sycl.cpp:40).
+__global__ void split_planes_kernel(const double* __restrict__ src, int64_t rows, int64_t k, int64_t ld_src,
+                                    int64_t kp, int mask5, __nv_bfloat16* __restrict__ planes) {
+  const int64_t n = rows * kp;
+  const int64_t plane = rows * kp;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / kp, c = i - r * kp;
+    double a = 0.0;
+    if (c < k) {
+      a = src[r * ld_src + c];
+      if (mask5) {
+        const int comp = (int)(r % 5);
+        if (comp != 0 && src[(r - comp) * ld_src + c] == 0.0) a = 0.0;
+      }
+    }
+    __nv_bfloat16 h, m, l;
+    split3(a, h, m, l);
+    planes[i] = h;
+    planes[plane + i] = m;
+    planes[2 * plane + i] = l;
+  }
+}
+
+// ------------------------------------------------------------------ PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.b32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: true when the phase completed, false after ~1 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (clock64() - t0 > kWaitCycles) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor for a K-major operand in the 128B-swizzled layout that
+// TMA writes: rows of 128 bytes, 8-row groups 1024 bytes apart.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: next 8-row group
+  d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;            // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+struct TileArgs {
+  double* out;       // [rows][ldo]
+  int64_t rows;      // valid rows
+  int64_t cols;      // valid columns (MO count)
+  int64_t ldo;
+  int kblocks;       // Kp / 64
+  int n_tile;        // columns per tile (multiple of 16, <= kMaxN)
+  uint32_t tmem_cols;
+  int* error;        // set to a non-zero code on a wait timeout
+};
+
+// Correction terms (A plane, B plane): hi*mid, mid*hi, hi*lo, mid*mid, lo*hi.
+__constant__ int kPairA[5] = {0, 1, 0, 1, 2};
+__constant__ int kPairB[5] = {1, 0, 2, 1, 0};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
+          taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15])));
+}
+
+// Bounded wait that also gives up once another role has aborted.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  const long long t0 = clock64();
+  while (!mbar_try(bar, parity)) {
+    if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void set_abort(volatile int* abort_flag, int* error, int code) {
+  *abort_flag = 1;
+  atomicExch(error, code);
+}
+
+// Tensor-memory columns: [0,N) corrections, [N,2N) and [2N,3N) main product ping-pong
+// buffers (one 64-wide K block each), [3N,4N) and [4N,5N) the running FP32 two-sum (hi, lo)
+// of the main product, folded in by the epilogue warps after every K block.
+__global__ void __launch_bounds__(kThreads, 1)
+    split_gemm_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
+                      const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
+                      const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2, TileArgs p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const uint32_t plane_b = (uint32_t)p.n_tile * kBK * 2;
+  const uint32_t stage_bytes = 3 * kPlaneA + 3 * plane_b;
+  uint64_t* full = (uint64_t*)(base + kStages * stage_bytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* accf = empty + kStages;  // [2] main buffer filled (MMA -> epilogue)
+  uint64_t* acce = accf + 2;         // [2] main buffer folded (epilogue -> MMA)
+  uint64_t* mma_done = acce + 2;
+  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kBM;
+  const int n0 = blockIdx.y * p.n_tile;
+  const int N = p.n_tile;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(p.tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const CUtensorMap* ta[3] = {&ta0, &ta1, &ta2};
+      const CUtensorMap* tb[3] = {&tb0, &tb1, &tb2};
+      int issued = 0;
+      bool ok = true;
+      for (int kb = 0; kb < p.kblocks; ++kb) {
+        const int s = kb % kStages;
+        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+        if (!wait_or_abort(&empty[s], ph ^ 1u, abort_flag)) {
+          ok = false;
+          set_abort(abort_flag, p.error, 1);
+          break;
+        }
+        unsigned char* st = base + s * stage_bytes;
+        mbar_expect_tx(&full[s], stage_bytes);
+        for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, ta[i], kb * kBK, m0, &full[s]);
+        for (int i = 0; i < 3; ++i) tma_load_2d(st + 3 * kPlaneA + i * plane_b, tb[i], kb * kBK, n0, &full[s]);
+        issued = kb + 1;
+      }
+      if (!ok) {
+        // drain the loads still in flight before the CTA's shared memory is released
+        for (int kb = issued - kStages < 0 ? 0 : issued - kStages; kb < issued; ++kb)
+          mbar_wait(&full[kb % kStages], (uint32_t)(kb / kStages) & 1u);
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+                             ((uint32_t)(kBM >> 4) << 24);
+      for (int kb = 0; kb < p.kblocks; ++kb) {
+        const int s = kb % kStages, b = kb & 1, use = kb >> 1;
+        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+        if (use > 0 && !wait_or_abort(&acce[b], (uint32_t)(use - 1) & 1u, abort_flag)) {
+          set_abort(abort_flag, p.error, 2);
+          break;
+        }
+        if (!wait_or_abort(&full[s], ph, abort_flag)) {
+          set_abort(abort_flag, p.error, 3);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t sa = smem_u32(base + s * stage_bytes);
+        const uint32_t sb = sa + 3 * kPlaneA;
+        const uint32_t main_acc = tmem + (uint32_t)((1 + b) * N);
+#pragma unroll
+        for (int kk = 0; kk < kBK / 16; ++kk) {
+          umma_bf16(main_acc, sdesc(sa + kk * 32), sdesc(sb + kk * 32), idesc, kk > 0 ? 1u : 0u);
+#pragma unroll
+          for (int t = 0; t < 5; ++t) {
+            const uint64_t ad = sdesc(sa + kPairA[t] * kPlaneA + kk * 32);
+            const uint64_t bd = sdesc(sb + kPairB[t] * plane_b + kk * 32);
+            umma_bf16(tmem, ad, bd, idesc, (kb | kk | t) != 0);
+          }
+        }
+        umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
+        umma_commit(&accf[b]);   // main buffer b holds this block's product
+      }
+      umma_commit(mma_done);  // every MMA this thread issued has completed
+    }
+  } else {
+    // epilogue: warp w owns TMEM lanes 32*(w % 4) .. +31 (one output row per thread)
+    const int quarter = warp & 3;
+    const int64_t row = (int64_t)m0 + quarter * 32 + lane;
+    const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
+    const uint32_t hi_col = 3 * N, lo_col = 4 * N;
+    bool ok = true;
+    for (int kb = 0; kb < p.kblocks; ++kb) {
+      const int b = kb & 1, use = kb >> 1;
+      if (!wait_or_abort(&accf[b], (uint32_t)use & 1u, abort_flag)) {
+        set_abort(abort_flag, p.error, 4);
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16], hi[16], lo[16];
+        tmem_ld16(lb + (uint32_t)((1 + b) * N + c0), v);
+        if (kb == 0) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            hi[j] = v[j];
+            lo[j] = 0.f;
+          }
+        } else {
+          tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
+          tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float s2, e2;
+            two_sum(hi[j], v[j], s2, e2);
+            hi[j] = s2;
+            lo[j] += e2;
+          }
+        }
+        tmem_st16(lb + hi_col + (uint32_t)c0, hi);
+        tmem_st16(lb + lo_col + (uint32_t)c0, lo);
+      }
+      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
+    }
+    if (ok) {
+      // the last accf phase covered every MMA, corrections included
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float c[16], hi[16], lo[16];
+        tmem_ld16(lb + (uint32_t)c0, c);
+        tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
+        tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
+        if (row < p.rows) {
+          double* o = p.out + row * p.ldo + n0 + c0;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            float s2, e2;
+            two_sum(hi[j], c[j], s2, e2);
+            if (n0 + c0 + j < p.cols) o[j] = f32_to_f64_int(s2) + f32_to_f64_int(lo[j] + e2);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    // no MMA may still be writing tensor memory when it is released
+    if (lane == 0) mbar_wait(mma_done, 0);
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols));
+  }
+}
+
+// ------------------------------------------------------------------ host side
+bool encode_map(CUtensorMap* map, const void* base, int64_t rows, int64_t kp, int box_rows) {
+  cuuint64_t dims[2] = {(cuuint64_t)kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides,
+                                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+cudaError_t launch_split(Ctx* ctx, const double* src, int64_t rows, int64_t k, int64_t ld, int64_t kp, bool mask5,
+                         __nv_bfloat16* planes) {
+  const int64_t n = rows * kp;
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  LaunchScope scope(ctx, mask5 ? "split_ao_planes" : "split_planes");
+  split_planes_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rows, k, ld, kp, mask5 ? 1 : 0, planes);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Splits (once per coefficient set) the MO coefficients [mo][ao] into BF16 planes.
+static qmckl_exit_code_device ensure_coef_planes(Ctx* ctx, qmckl_context_device c, int64_t kp) {
+  MoBasisData& mo = ctx->mo_basis;
+  if (mo.coef_split && mo.split_ao_pad == kp && mo.split_mo_pad == mo.mo_num) return QMCKL_SUCCESS_DEVICE;
+  if (mo.coef_split) dfree(ctx, mo.coef_split);
+  mo.coef_split = dalloc(ctx, sizeof(__nv_bfloat16) * 3 * mo.mo_num * kp);
+  if (!mo.coef_split) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, "qmckl_provide_mo_basis_mo_vgl_device", nullptr);
+  mo.split_ao_pad = kp;
+  mo.split_mo_pad = mo.mo_num;
+  launch_split(ctx, mo.coefficient, mo.mo_num, ctx->ao_basis.ao_num, ctx->ao_basis.ao_num, kp, false,
+               static_cast<__nv_bfloat16*>(mo.coef_split));
+  return finish(ctx, c, "qmckl_provide_mo_basis_mo_vgl_device");
+}
+
+// out[rows][M] = split-BF16 product of src[rows][A] (FP64, ld = A) and the coefficients.
+qmckl_exit_code_device split_contract(Ctx* ctx, qmckl_context_device c, const double* src, int64_t rows, bool mask5,
+                                      double* out) {
+  const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
+  MoBasisData& mo = ctx->mo_basis;
+  const int64_t A = ctx->ao_basis.ao_num, M = mo.mo_num;
+  if (rows <= 0 || M <= 0) return QMCKL_SUCCESS_DEVICE;
+  const int64_t kp = round_up(A, kBK);
+  if (kp / kBK > (int64_t)INT32_MAX || rows > (int64_t)INT32_MAX - kBM)
+    return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
+  qmckl_exit_code_device rc = ensure_coef_planes(ctx, c, kp);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  const size_t need = sizeof(__nv_bfloat16) * 3 * (size_t)rows * (size_t)kp + 256;
+  if (!ensure_raw(ctx, &mo.ao_split, &mo.ao_split_cap, need))
+    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
+  __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
+  // error word lives after the planes
+  int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(mo.ao_split) + need - 256);
+  launch_split(ctx, src, rows, A, A, kp, mask5, ap);
+  cudaMemsetAsync(err, 0, sizeof(int), ctx->stream);
+
+  const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
+  const int n_tile = (int)round_up((M + ntiles - 1) / ntiles, 16);
+  uint32_t tcols = 32;
+  while ((int)tcols < 5 * n_tile) tcols *= 2;
+  CUtensorMap ta[3], tb[3];
+  const __nv_bfloat16* bp = static_cast<const __nv_bfloat16*>(mo.coef_split);
+  for (int i = 0; i < 3; ++i) {
+    if (!encode_map(&ta[i], ap + (size_t)i * rows * kp, rows, kp, kBM) ||
+        !encode_map(&tb[i], bp + (size_t)i * M * kp, M, kp, n_tile))
+      return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
+  }
+  TileArgs args;
+  args.out = out;
+  args.rows = rows;
+  args.cols = M;
+  args.ldo = M;
+  args.kblocks = (int)(kp / kBK);
+  args.n_tile = n_tile;
+  args.tmem_cols = tcols;
+  args.error = err;
+  const size_t smem = 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)n_tile * kBK * 2) + 256;
+  cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid((unsigned)((rows + kBM - 1) / kBM), (unsigned)ntiles);
+  {
+    LaunchScope scope(ctx, mask5 ? "mo_vgl_split_bf16" : "mo_value_split_bf16");
+    split_gemm_kernel<<<grid, kThreads, smem, ctx->stream>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], args);
+  }
+  rc = finish(ctx, c, fn);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  if (!ctx->async) {
+    int h = 0;
+    cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (h) return fail(c, QMCKL_FAILURE_DEVICE, fn, "split-BF16 GEMM: a pipeline wait timed out");
+  }
+  return QMCKL_SUCCESS_DEVICE;
+}
 
 qmckl_exit_code_device provide_mo_split(Ctx* ctx, qmckl_context_device c, double* dst, bool value_only) {
-  (void)ctx;
-  (void)dst;
-  (void)value_only;
-  return fail(c, QMCKL_FAILURE_DEVICE, "qmckl_provide_mo_basis_mo_vgl_device", "split-BF16 form not available");
+  if (value_only)
+    return split_contract(ctx, c, ctx->ao_basis.ao_value, ctx->point.num, false, dst);
+  return split_contract(ctx, c, ctx->ao_basis.ao_vgl, 5 * ctx->point.num, true, dst);
 }
 
 }  // namespace qg

@@ -1,0 +1,70 @@
+"""Precision form: MO contraction as a split-BF16 product on the tcgen05 tensor cores
+(three BF16 terms per FP64 operand, six cross products, FP32 accumulation). Target:
+MO vgl within 1e-6 relative of the FP64 oracle, normwise per component; the AO arrays
+(FP64 throughout) stay within the FP64 tolerance."""
+import numpy as np
+import pytest
+
+from conftest import normwise_rel_err
+from oracle import oracle
+from qmckl_sycl_gb300 import PRECISION_FP64, PRECISION_SPLIT_BF16, Context, config_adjoint, config_medium, config_small
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RTOL = 1e-6
+
+
+def run(s, mode):
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(mode)
+        P = s.point_num
+        return dict(ao_vgl=ctx.get_ao_vgl(P), mo_vgl=ctx.get_mo_vgl(P), mo_value=ctx.get_mo_value(P))
+
+
+@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium_sub"])
+def test_split_mo_vgl_within_1e6(name, chbrclf):
+    s = {"chbrclf": lambda: chbrclf, "small": lambda: config_small(0), "adjoint": lambda: config_adjoint(0),
+         "medium_sub": lambda: config_medium(0, walkers=8, electrons=160)}[name]()
+    ref = oracle.forward(s, want=("ao_vgl", "mo_vgl", "mo_value"))
+    out = run(s, PRECISION_SPLIT_BF16)
+    assert normwise_rel_err(out["ao_vgl"], ref["ao_vgl"]) <= 1e-12
+    errs = [normwise_rel_err(out["mo_vgl"][:, c:c + 1], ref["mo_vgl"][:, c:c + 1]) for c in range(5)]
+    print("%s split-BF16 mo_vgl normwise rel err per component: %s" % (name, " ".join("%.2e" % e for e in errs)))
+    assert max(errs) <= MIXED_RTOL
+    assert normwise_rel_err(out["mo_value"], ref["mo_value"]) <= MIXED_RTOL
+
+
+def test_split_respects_zero_value_skip():
+    s = config_small(4, point_num=8)
+    coord = s.coord.copy()
+    coord[:, 0] = s.nucl_coord[0, 0]
+    s = s.with_points(coord)
+    ref = oracle.forward(s, want=("mo_vgl",))
+    out = run(s, PRECISION_SPLIT_BF16)
+    assert normwise_rel_err(out["mo_vgl"], ref["mo_vgl"]) <= MIXED_RTOL
+
+
+def test_mode_switch_recomputes(chbrclf):
+    s = chbrclf
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        a = ctx.get_mo_vgl(s.point_num)
+        ctx.set_precision(PRECISION_SPLIT_BF16)
+        b = ctx.get_mo_vgl(s.point_num)
+        ctx.set_precision(PRECISION_FP64)
+        c = ctx.get_mo_vgl(s.point_num)
+    assert not np.array_equal(a, b)  # the split product rounds differently
+    assert np.array_equal(a, c)
+    assert normwise_rel_err(b, a) <= MIXED_RTOL
+
+
+@pytest.mark.parametrize("mo_num", [1, 17, 160, 161, 333])
+def test_split_tile_edges(mo_num):
+    s = config_small(9, point_num=77)
+    rng = np.random.default_rng(mo_num)
+    s = s.__class__(**{**s.__dict__, "mo_num": mo_num, "mo_coef": rng.normal(0, 1 / np.sqrt(s.ao_num),
+                                                                              size=(mo_num, s.ao_num))})
+    ref = oracle.forward(s, want=("mo_vgl",))
+    out = run(s, PRECISION_SPLIT_BF16)
+    assert normwise_rel_err(out["mo_vgl"], ref["mo_vgl"]) <= MIXED_RTOL
