@@ -162,3 +162,11 @@ def test_lock_is_recursive():
     L.qmckl_unlock_device(c)
     L.qmckl_unlock_device(c)
     L.qmckl_context_destroy_device(c)
+
+
+def test_library_does_not_need_the_driver_library():
+    # the library must load on machines without a GPU driver (driver entry points are
+    # resolved at run time through the CUDA runtime)
+    out = subprocess.check_output(["readelf", "-d", capi.LIB_PATH]).decode()
+    needed = [line.split("[")[-1].rstrip("]") for line in out.splitlines() if "(NEEDED)" in line]
+    assert not any(n.startswith("libcuda.so") for n in needed), needed
