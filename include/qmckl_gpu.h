@@ -320,6 +320,38 @@ qmckl_exit_code_device qmckl_host_unregister_device(qmckl_context_device context
  * register-resident mma loop over every SM (a roofline denominator for the FP64 form). */
 qmckl_exit_code_device qmckl_measure_fp64_peak_device(qmckl_context_device context, double* tflops);
 
+/* Split-BF16 MO contraction that allocates nothing (no counterpart in the reference).
+ *
+ *   out[r][m] = sum_k ao[r][k] * coefficient[m][k]      (r < rows, m < mo_num)
+ *
+ * with the same split-BF16 tensor-core product as QMCKL_PRECISION_SPLIT_BF16_DEVICE. It is
+ * meant for callers that must not have device memory allocated behind their back: codes
+ * whose own pool allocator owns the GPU's memory, hosts that load this library as a plug-in
+ * and forbid it to allocate, and loops where a cudaMalloc/cudaFree would synchronise the
+ * device. The caller passes every input and output (device pointers: ao [rows][ao_num] FP64,
+ * coefficient [mo_num][ao_num] FP64 in the reference's layout, out [rows][mo_num] FP64); the
+ * scratch space (BF16 operand planes) is a 28 MiB device array compiled into the library,
+ * which every GPU that loads the library keeps until the process exits. No cudaMalloc,
+ * cudaFree or other allocating routine is called.
+ *
+ * Limits set by that array: 1 <= ao_num <= 2048 (else QMCKL_INVALID_ARG_3_DEVICE) and
+ * 1 <= mo_num <= 1024 (else QMCKL_INVALID_ARG_5_DEVICE); rows is unbounded (processed in
+ * chunks). With vgl_mask = 1, rows are ao_vgl rows (5 per point: value, d/dx, d/dy, d/dz,
+ * Laplacian; rows % 5 == 0 else QMCKL_INVALID_ARG_2_DEVICE) and an AO whose value is exactly
+ * zero is dropped from that point's four derivative rows too, as the reference's MO kernel
+ * does; with vgl_mask = 0 every row is used as is (ao_value rows). NULL pointers give
+ * QMCKL_INVALID_ARG_1/4/7_DEVICE. Work is issued on cuda_stream (a cudaStream_t; NULL for the
+ * legacy default stream) and the call waits for it; a pipeline stall in the kernel returns
+ * QMCKL_FAILURE_DEVICE.
+ *
+ * The first call on a device resolves the array's device address for that device (with that
+ * device current); make that first call before any stream capture. All calls share the one
+ * array, so calls whose work overlaps on the GPU (different streams, or concurrent host
+ * threads) race on it: serialise them. */
+qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(const double* ao, int64_t rows, int64_t ao_num,
+                                                                   const double* coefficient, int64_t mo_num,
+                                                                   int32_t vgl_mask, double* out, void* cuda_stream);
+
 /* Test hook for allocation failure handling: the n-th device allocation from now on
  * (n >= 1) fails as if cudaMalloc had failed; n = 0 disables the hook. */
 qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device context, int64_t n);

@@ -540,3 +540,127 @@ qmckl_exit_code_device provide_mo_split(Ctx* ctx, qmckl_context_device c, double
 }
 
 }  // namespace qg
+
+// ======================================================================================
+// Split-BF16 contraction that allocates nothing.
+//
+// Some callers cannot let a library allocate device memory: codes that hand all device
+// memory to their own pool allocator at start-up (a cudaMalloc from a library then fails or
+// fragments the pool), hosts that load this library as a plug-in and forbid it to allocate
+// on its own, and latency-critical loops where cudaMalloc/cudaFree would synchronise the
+// device and stall other streams. For them this entry point keeps its scratch memory (the
+// BF16 operand planes and an error word) in the file-scope device array below, which every
+// GPU that loads the library holds until the process exits. Its size bounds the problem:
+// ao_num <= 2048 and mo_num <= 1024; any number of rows is accepted (rows are processed in
+// chunks of kNoAllocChunkRows that reuse the array in stream order).
+// ======================================================================================
+namespace qg {
+namespace {
+
+constexpr int64_t kNoAllocMaxAo = 2048;
+constexpr int64_t kNoAllocMaxMo = 1024;
+constexpr int64_t kNoAllocChunkRows = 1280;  // a multiple of 128 (tile rows) and of 5 (vgl rows of a point)
+constexpr size_t kNoAllocBytes =
+    sizeof(__nv_bfloat16) * 3 * (size_t)(kNoAllocMaxMo + kNoAllocChunkRows) * (size_t)kNoAllocMaxAo + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Host-side device addresses of the array, one per device, resolved on each device's first
+// call (with that device current). A host pointer to the symbol is not a device address.
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+}  // namespace qg
+
+extern "C" qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(const double* ao, int64_t rows,
+                                                                              int64_t ao_num,
+                                                                              const double* coefficient,
+                                                                              int64_t mo_num, int32_t vgl_mask,
+                                                                              double* out, void* cuda_stream) {
+  using namespace qg;
+  if (!ao) return QMCKL_INVALID_ARG_1_DEVICE;
+  if (rows < 0 || (vgl_mask && rows % 5 != 0)) return QMCKL_INVALID_ARG_2_DEVICE;
+  if (ao_num < 1 || ao_num > kNoAllocMaxAo) return QMCKL_INVALID_ARG_3_DEVICE;
+  if (!coefficient) return QMCKL_INVALID_ARG_4_DEVICE;
+  if (mo_num < 1 || mo_num > kNoAllocMaxMo) return QMCKL_INVALID_ARG_5_DEVICE;
+  if (vgl_mask != 0 && vgl_mask != 1) return QMCKL_INVALID_ARG_6_DEVICE;
+  if (!out) return QMCKL_INVALID_ARG_7_DEVICE;
+  if (rows == 0) return QMCKL_SUCCESS_DEVICE;
+  cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+    cudaGetLastError();
+    return QMCKL_FAILURE_DEVICE;
+  }
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return QMCKL_FAILURE_DEVICE;
+      }
+      g_noalloc_ptr[dev] = p;
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+
+  const int64_t kp = round_up(ao_num, kBK);
+  const int64_t M = mo_num;
+  __nv_bfloat16* bplanes = static_cast<__nv_bfloat16*>(scratch);
+  __nv_bfloat16* aplanes = bplanes + 3 * M * kp;
+  int* err = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + kNoAllocBytes - 256);
+  if (cudaMemsetAsync(err, 0, sizeof(int), stream) != cudaSuccess) {
+    cudaGetLastError();
+    return QMCKL_FAILURE_DEVICE;
+  }
+
+  const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
+  const int n_tile = (int)round_up((M + ntiles - 1) / ntiles, 16);
+  uint32_t tcols = 32;
+  while ((int)tcols < 5 * n_tile) tcols *= 2;
+  const size_t smem = 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)n_tile * kBK * 2) + 256;
+  cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+
+  auto split = [&](const double* src, int64_t n, int64_t ld, bool mask, __nv_bfloat16* dst) {
+    int64_t blocks = (n * kp + 255) / 256;
+    if (blocks > 152 * 64) blocks = 152 * 64;
+    split_planes_kernel<<<(unsigned)blocks, 256, 0, stream>>>(src, n, ao_num, ld, kp, mask ? 1 : 0, dst);
+  };
+  split(coefficient, M, ao_num, false, bplanes);
+  CUtensorMap tb[3];
+  for (int i = 0; i < 3; ++i)
+    if (!encode_map(&tb[i], bplanes + (size_t)i * M * kp, M, kp, n_tile)) return QMCKL_FAILURE_DEVICE;
+
+  for (int64_t r0 = 0; r0 < rows; r0 += kNoAllocChunkRows) {
+    const int64_t n = rows - r0 < kNoAllocChunkRows ? rows - r0 : kNoAllocChunkRows;
+    split(ao + r0 * ao_num, n, ao_num, vgl_mask != 0, aplanes);
+    CUtensorMap ta[3];
+    for (int i = 0; i < 3; ++i)
+      if (!encode_map(&ta[i], aplanes + (size_t)i * n * kp, n, kp, kBM)) return QMCKL_FAILURE_DEVICE;
+    TileArgs args;
+    args.out = out + r0 * M;
+    args.rows = n;
+    args.cols = M;
+    args.ldo = M;
+    args.kblocks = (int)(kp / kBK);
+    args.n_tile = n_tile;
+    args.tmem_cols = tcols;
+    args.error = err;
+    dim3 grid((unsigned)((n + kBM - 1) / kBM), (unsigned)ntiles);
+    split_gemm_kernel<<<grid, kThreads, smem, stream>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], args);
+  }
+  int h = 0;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess) {
+    cudaGetLastError();
+    return QMCKL_FAILURE_DEVICE;
+  }
+  return h ? QMCKL_FAILURE_DEVICE : QMCKL_SUCCESS_DEVICE;
+}
