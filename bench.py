@@ -347,14 +347,15 @@ def main():
     def roof(form):
         st = results[form]["stats"]
         out = {}
-        if st.get("ao_vgl_fused", (0, 0))[0] > 0:
-            n, tot = st["ao_vgl_fused"]
-            ms = tot / max(n, 1)
-            alg = 8.0 * (5 * A + 3) * P
-            out["ao_vgl_fused"] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9,
-                                   "peak": peaks["hbm_gbs"], "unit": "GB/s", "ms_per_launch": ms,
-                                   "traffic": traffic.get("ao_vgl_fused", 0) * P or None}
-            out["ao_vgl_fused"]["frac"] = out["ao_vgl_fused"]["achieved"] / peaks["hbm_gbs"]
+        # AO kernel: FP64 ao_vgl (8 bytes per element) or the three BF16 planes (6 bytes)
+        for k, per_elem in (("ao_vgl_fused", 8.0), ("ao_vgl_fused_bf16_planes", 6.0)):
+            if st.get(k, (0, 0))[0] > 0:
+                n, tot = st[k]
+                ms = tot / max(n, 1)
+                alg = (per_elem * 5 * A + 24.0) * P
+                out[k] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
+                          "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
+                out[k]["frac"] = out[k]["achieved"] / peaks["hbm_gbs"]
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
             if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]

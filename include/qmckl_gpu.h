@@ -320,6 +320,12 @@ qmckl_exit_code_device qmckl_host_unregister_device(qmckl_context_device context
  * register-resident mma loop over every SM (a roofline denominator for the FP64 form). */
 qmckl_exit_code_device qmckl_measure_fp64_peak_device(qmckl_context_device context, double* tflops);
 
+/* Validation of the exponential the fused AO kernel evaluates (a table-driven method for
+ * arguments in the screened range): for device arrays x[n] with 0 <= x[i] <= 27.7, writes
+ * out[2i] = the kernel's e^-x[i] and out[2i+1] = CUDA's exp(-x[i]). Needs a finalized AO
+ * basis (QMCKL_NOT_PROVIDED_DEVICE otherwise). */
+qmckl_exit_code_device qmckl_exp_check_device(qmckl_context_device context, const double* x, int64_t n, double* out);
+
 /* Split-BF16 MO contraction that allocates nothing (no counterpart in the reference).
  *
  *   out[r][m] = sum_k ao[r][k] * coefficient[m][k]      (r < rows, m < mo_num)

@@ -69,6 +69,8 @@ void free_tables(Ctx* ctx, AoTables& t) {
   dfree(ctx, t.shell_orig);
   dfree(ctx, t.shell_nucl);
   dfree(ctx, t.chunks);
+  dfree(ctx, t.exp_table);
+  t.exp_table = nullptr;
   t.nuclei = nullptr;
   t.shells = nullptr;
   t.prims = nullptr;
@@ -197,6 +199,30 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
     if (p >= N) break;
   }
   t.h_ao_factor = aof;
+  // 2^(j/32) to ~64 bits: hi = nearest double, lo = remainder (long double on the host)
+  std::vector<ExpTable> et(1);
+  for (int j = 0; j < 32; ++j) {
+    const long double v = exp2l((long double)j / 32.0L);
+    et[0].hi[j] = (double)v;
+    et[0].lo[j] = (double)(v - (long double)et[0].hi[j]);
+  }
+  // point-grouping grid over the nuclei plus a 4-bohr margin, 32 cells along the longest side
+  {
+    double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
+    for (int64_t n = 0; n < N; ++n)
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], ncoord[d * N + n]);
+        hi[d] = std::max(hi[d], ncoord[d * N + n]);
+      }
+    const double margin = 4.0;
+    double ext = 0.0;
+    for (int d = 0; d < 3; ++d) {
+      t.grid_origin[d] = std::isfinite(lo[d]) ? lo[d] - margin : 0.0;
+      ext = std::max(ext, std::isfinite(hi[d] - lo[d]) ? hi[d] - lo[d] + 2 * margin : 0.0);
+    }
+    const double cell = std::max(ext / 32.0, 0.25);
+    t.grid_inv_cell = 1.0 / cell;
+  }
   t.nucl_num = (int32_t)N;
   t.shell_num = (int32_t)t.h_shells.size();
   t.prim_num = (int32_t)t.h_prims.size();
@@ -214,7 +240,9 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   t.shell_orig = to_device(ctx, t.h_shell_orig);
   t.shell_nucl = to_device(ctx, t.h_shell_nucl);
   t.chunks = to_device(ctx, t.h_chunks);
-  if (!t.nuclei || !t.shells || !t.prims || !t.ao_factor || !t.shell_orig || !t.shell_nucl || !t.chunks) {
+  t.exp_table = to_device(ctx, et);
+  if (!t.nuclei || !t.shells || !t.prims || !t.ao_factor || !t.shell_orig || !t.shell_nucl || !t.chunks ||
+      !t.exp_table) {
     free_tables(ctx, t);
     return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "kernel tables");
   }
@@ -232,6 +260,34 @@ qmckl_exit_code_device ensure_tables(Ctx* ctx, qmckl_context_device c) {
     return fail(c, QMCKL_FAILURE_DEVICE, "compute_ao_basis_shell_vgl", "Not yet implemented for basis type != 'G'");
   if (ctx->ao_basis.tables.valid) return QMCKL_SUCCESS_DEVICE;
   return build_tables(ctx, c);
+}
+
+// The processing order of the current points for the fused AO kernels (recomputed when the
+// point set changes).
+const int32_t* point_order(Ctx* ctx) {
+  AoBasisData& ao = ctx->ao_basis;
+  const int64_t P = ctx->point.num;
+  if (P <= 0 || P > (int64_t)INT32_MAX - 64) return nullptr;
+  if (ao.point_perm && ao.perm_date == ctx->point.date) return ao.point_perm;
+  void* perm = ao.point_perm;
+  void* keys = ao.point_keys;
+  void* counts = ao.cell_counts;
+  if (!ensure_raw(ctx, &perm, &ao.perm_cap, sizeof(int32_t) * P) ||
+      !ensure_raw(ctx, &keys, &ao.keys_cap, sizeof(int32_t) * P) ||
+      !ensure_raw(ctx, &counts, &ao.counts_cap, sizeof(int32_t) * kOrderCells)) {
+    ao.point_perm = static_cast<int32_t*>(perm);
+    ao.point_keys = static_cast<int32_t*>(keys);
+    ao.cell_counts = static_cast<int32_t*>(counts);
+    return nullptr;  // fall back to the identity order
+  }
+  ao.point_perm = static_cast<int32_t*>(perm);
+  ao.point_keys = static_cast<int32_t*>(keys);
+  ao.cell_counts = static_cast<int32_t*>(counts);
+  if (launch_point_order(ctx, ao.tables, ctx->point.coord, P, ao.point_keys, ao.cell_counts, ao.point_perm) !=
+      cudaSuccess)
+    return nullptr;
+  ao.perm_date = ctx->point.date;
+  return ao.point_perm;
 }
 
 // Clears the AO and MO caches (after a basis change).
@@ -661,8 +717,7 @@ qmckl_exit_code_device qmckl_provide_ao_basis_shell_vgl_device(qmckl_context_dev
 static qmckl_exit_code_device compute_ao_vgl(Ctx* ctx, qmckl_context_device context, double* dst, const char* fn) {
   qmckl_exit_code_device rc = ensure_tables(ctx, context);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
-  if (launch_ao_vgl(ctx, ctx->ao_basis.tables, ctx->point.coord, ctx->point.num, dst) != cudaSuccess)
-    return finish(ctx, context, fn);
+  launch_ao_vgl(ctx, ctx->ao_basis.tables, ctx->point.coord, point_order(ctx), ctx->point.num, dst);
   return finish(ctx, context, fn);
 }
 
@@ -675,7 +730,7 @@ static qmckl_exit_code_device compute_ao_value(Ctx* ctx, qmckl_context_device co
   }
   qmckl_exit_code_device rc = ensure_tables(ctx, context);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
-  launch_ao_value(ctx, ao.tables, ctx->point.coord, ctx->point.num, dst);
+  launch_ao_value(ctx, ao.tables, ctx->point.coord, point_order(ctx), ctx->point.num, dst);
   return finish(ctx, context, fn);
 }
 

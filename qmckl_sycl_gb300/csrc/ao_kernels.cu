@@ -1,6 +1,7 @@
 // Fused AO kernels for sm_103a: electron-nucleus displacement, exponent-cutoff screening,
 // Gaussian shell radials, Cartesian polynomial and AO assembly in one pass, writing
-// ao_vgl[point][5][ao] (or ao_value[point][ao]) without any intermediate global array.
+// ao_vgl[point][5][ao] (or ao_value[point][ao], or the BF16 planes of the split-BF16 MO
+// contraction) without any intermediate global array.
 //
 // Reference computation (qmckl_sycl): shell radials src/qmckl_ao_sycl.cpp:40-95, the
 // polynomial kernel :195-334 and the assembly kernel :337-422 (value-only :438-740),
@@ -12,13 +13,20 @@
 //  * one lane per point: every lane of a warp walks the same nucleus/shell/primitive/AO
 //    sequence, so table loads are warp-uniform broadcasts and every FP64 instruction
 //    runs with all 32 lanes busy;
+//  * points are processed in an order that puts spatial neighbours in the same warp
+//    (launch_point_order), because a primitive's exponential is evaluated when any lane
+//    of the warp needs it: on the medium workload this cuts the exponentials per point
+//    from 65 % to 36 % of the primitives (30 % is the per-lane share);
 //  * screening costs no FP64 instruction: the reference's tests `r2 > cutoff*range`
 //    and `expo*r2 > cutoff` are replaced by unsigned compares of bit patterns against
 //    thresholds precomputed on the host (for non-negative doubles the bit order is the
 //    numeric order, and fl(expo*r2) is monotone in r2), which gives the reference's
-//    decisions exactly; an exponential is only evaluated when some lane needs it;
+//    decisions exactly;
 //  * r2 is formed with the reference's rounding ((x*x + y*y) + z*z, no fused
 //    multiply-add), so the screening inputs are the reference's bits;
+//  * the exponential is evaluated with Tang's table-driven method on the screened range
+//    x in [-27.64, 0] (12 FP64 instructions: reduction by ln2/32, a degree-6 polynomial, a
+//    32-entry table of 2^(j/32) in shared memory, exponent scaling by integer addition);
 //  * the radial derivatives are accumulated as g = sum(-2 a v) and h = sum(-2 a v a r2)
 //    (two accumulators instead of four) and the Laplacian assembly uses Euler's identity
 //    x.dP/dx + y.dP/dy + z.dP/dz = l P for the degree-l monomial P, so that
@@ -27,7 +35,9 @@
 //  * Cartesian components are specialised at compile time for l <= 3 (products with
 //    0 and 1 fold away); higher l takes a generic path;
 //  * results are staged per warp in shared memory and stored as contiguous row
-//    segments of ao_vgl, so global stores are coalesced whatever the point order.
+//    segments, so global stores are coalesced whatever the point order.
+#include <cuda_bf16.h>
+
 #include <cstdint>
 
 #include "internal.hpp"
@@ -40,25 +50,62 @@ constexpr int kStage = 8;          // AOs staged per warp between flushes
 constexpr int kPad = 33;           // 32 points + 1 (bank-conflict padding), in doubles
 constexpr unsigned kFull = 0xffffffffu;
 
+enum class Out { Vgl, Value, Planes };
+template <Out O>
+__host__ __device__ constexpr int ncomp() {
+  return O == Out::Value ? 1 : 5;
+}
+
 template <int NC>
 struct Stage {
   double v[NC][kStage][kPad];
+  int64_t pidx[32];  // point index of each lane (-1: no point)
 };
 
 __device__ __forceinline__ uint64_t bits_of(double x) { return static_cast<uint64_t>(__double_as_longlong(x)); }
 __device__ __forceinline__ bool is_one(double f) { return bits_of(f) == 0x3FF0000000000000ull; }
 
+// ---------------------------------------------------------------- exponential
+// e^(-x) for 0 <= x <= 27.7 (the screened range: fl(a r2) <= 27.631...), Tang's method:
+// x = (n/32) ln 2 + r with |r| <= ln2/64, e^-x = 2^(n>>5) * 2^((n&31)/32) * e^r.
+constexpr double kInvL = 46.166241308446828;               // 32 / ln 2 (only rounds n)
+constexpr double kShifter = 6755399441055744.0;            // 1.5 * 2^52: rounds to an integer
+constexpr double kL1 = 0.6931471805599453094 / 32.0;       // double nearest ln 2, / 32 (exact)
+constexpr double kL2 = 2.3190468138462996e-17 / 32.0;      // ln 2 - that double, / 32
+
+__device__ __forceinline__ double exp_neg(double x, const double* __restrict__ thi, const double* __restrict__ tlo) {
+  const double y = -x;
+  const double t = fma(y, kInvL, kShifter);
+  const int n = __double2loint(t);
+  const double nd = t - kShifter;
+  double r = fma(-nd, kL1, y);
+  r = fma(-nd, kL2, r);
+  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
+  p = fma(p, r, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(p, r, 1.0);
+  p = p * r;  // e^r - 1
+  const int j = n & 31, m = n >> 5;
+  const double th = thi[j];
+  const double res = fma(th, p, tlo[j]) + th;
+  return __longlong_as_double(__double_as_longlong(res) + ((long long)m << 52));
+}
+
+// ---------------------------------------------------------------- output staging
 // Collects one warp's AO values (lane = point) and writes them as row segments.
-template <int NC>
+template <Out O>
 struct Writer {
+  static constexpr int NC = ncomp<O>();
   Stage<NC>* st;
-  double* out;       // ao_vgl or ao_value
-  int64_t p0;        // first point of the warp
-  int64_t ao_num;
-  int nvalid;        // points of the warp that exist
+  double* out;               // ao_vgl / ao_value (Vgl, Value)
+  __nv_bfloat16* planes;     // Planes: [3][5P][row_len]
+  int64_t plane_stride;      // Planes: 5P * row_len
+  int64_t row_len;           // ao_num, or kp for Planes
+  int nvalid;                // points of the warp that exist
   int lane;
-  int base;          // AO index of stage slot 0
-  int fill;          // staged AOs
+  int base;                  // AO index of stage slot 0
+  int fill;                  // staged AOs
 
   __device__ __forceinline__ void flush() {
     __syncwarp();
@@ -68,7 +115,39 @@ struct Writer {
       const int rest = i / kStage;
       const int c = rest % NC;
       const int q = rest / NC;
-      if (j < fill) out[(p0 + q) * (NC * ao_num) + c * ao_num + base + j] = st->v[c][j][q];
+      if (j >= fill) continue;
+      const int64_t pt = st->pidx[q];
+      const double val = st->v[c][j][q];
+      if constexpr (O == Out::Planes) {
+        // the reference's MO kernel drops an AO whose value is exactly zero from every
+        // component of the point (src/qmckl_mo_sycl.cpp:40)
+        const double a = (c != 0 && st->v[0][j][q] == 0.0) ? 0.0 : val;
+        const int64_t o = (5 * pt + c) * row_len + base + j;
+        // split into three BF16 terms with integer and FP32 instructions (no FP64)
+        const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+        const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+        const int e = (int)((b >> 52) & 0x7FF) - 896;
+        float f;
+        if (e <= 0) {
+          f = __uint_as_float(sign);
+        } else {
+          const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+          const unsigned int mm = (unsigned int)(frac >> 29);
+          const unsigned long long rem = frac & 0x1FFFFFFFull;
+          unsigned int bits = ((unsigned int)(e < 255 ? e : 255) << 23) | (e < 255 ? mm : 0u);
+          if (e < 255 && (rem > 0x10000000ull || (rem == 0x10000000ull && (mm & 1u)))) bits += 1u;
+          f = __uint_as_float(sign | bits);
+        }
+        const __nv_bfloat16 h = __float2bfloat16_rn(f);
+        const float r1 = f - __bfloat162float(h);
+        const __nv_bfloat16 md = __float2bfloat16_rn(r1);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(md));
+        planes[o] = h;
+        planes[plane_stride + o] = md;
+        planes[2 * plane_stride + o] = lo;
+      } else {
+        out[pt * (NC * row_len) + c * row_len + base + j] = val;
+      }
     }
     __syncwarp();
     base += fill;
@@ -97,9 +176,10 @@ struct ShellVals {
 
 // One Cartesian component x^a y^b z^c (a, b, c compile-time), assembled like the
 // reference's src/qmckl_ao_sycl.cpp:371-420 and multiplied by the AO factor.
-template <int NC, int a, int b, int c>
-__device__ __forceinline__ void cart(Writer<NC>& w, const double (&X)[4], const double (&Y)[4], const double (&Z)[4],
+template <Out O, int a, int b, int c>
+__device__ __forceinline__ void cart(Writer<O>& w, const double (&X)[4], const double (&Y)[4], const double (&Z)[4],
                                      const ShellVals& s, double f, bool zero) {
+  constexpr int NC = ncomp<O>();
   const double yz = Y[b] * Z[c];
   const double P = X[a] * yz;
   double v[NC];
@@ -135,41 +215,42 @@ __device__ __forceinline__ void cart(Writer<NC>& w, const double (&X)[4], const 
 
 // Components of one shell in the reference's order: a descending, then b descending
 // (src/qmckl_ao_sycl.cpp:297-305).
-template <int NC, int L>
-__device__ __forceinline__ void shell_fixed(Writer<NC>& w, const double (&X)[4], const double (&Y)[4],
+template <Out O, int L>
+__device__ __forceinline__ void shell_fixed(Writer<O>& w, const double (&X)[4], const double (&Y)[4],
                                             const double (&Z)[4], const ShellVals& s, const double* __restrict__ aof,
                                             int ao0, bool zero) {
   if constexpr (L == 0) {
-    cart<NC, 0, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0), zero);
+    cart<O, 0, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0), zero);
   } else if constexpr (L == 1) {
-    cart<NC, 1, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
-    cart<NC, 0, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
-    cart<NC, 0, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 1, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
+    cart<O, 0, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
+    cart<O, 0, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
   } else if constexpr (L == 2) {
-    cart<NC, 2, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
-    cart<NC, 1, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
-    cart<NC, 1, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
-    cart<NC, 0, 2, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 3), zero);
-    cart<NC, 0, 1, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 4), zero);
-    cart<NC, 0, 0, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 5), zero);
+    cart<O, 2, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
+    cart<O, 1, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
+    cart<O, 1, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 0, 2, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 3), zero);
+    cart<O, 0, 1, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 4), zero);
+    cart<O, 0, 0, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 5), zero);
   } else {
-    cart<NC, 3, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
-    cart<NC, 2, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
-    cart<NC, 2, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
-    cart<NC, 1, 2, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 3), zero);
-    cart<NC, 1, 1, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 4), zero);
-    cart<NC, 1, 0, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 5), zero);
-    cart<NC, 0, 3, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 6), zero);
-    cart<NC, 0, 2, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 7), zero);
-    cart<NC, 0, 1, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 8), zero);
-    cart<NC, 0, 0, 3>(w, X, Y, Z, s, __ldg(aof + ao0 + 9), zero);
+    cart<O, 3, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
+    cart<O, 2, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
+    cart<O, 2, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 1, 2, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 3), zero);
+    cart<O, 1, 1, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 4), zero);
+    cart<O, 1, 0, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 5), zero);
+    cart<O, 0, 3, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 6), zero);
+    cart<O, 0, 2, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 7), zero);
+    cart<O, 0, 1, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 8), zero);
+    cart<O, 0, 0, 3>(w, X, Y, Z, s, __ldg(aof + ao0 + 9), zero);
   }
 }
 
 // Generic path for l >= 4 (rare): powers in local memory, same formulas.
-template <int NC>
-__device__ __noinline__ void shell_generic(Writer<NC>& w, double x, double y, double z, int L, const ShellVals& s,
+template <Out O>
+__device__ __noinline__ void shell_generic(Writer<O>& w, double x, double y, double z, int L, const ShellVals& s,
                                            const double* __restrict__ aof, int ao0, bool zero) {
+  constexpr int NC = ncomp<O>();
   double X[kMaxL + 1], Y[kMaxL + 1], Z[kMaxL + 1];
   X[0] = Y[0] = Z[0] = 1.0;
   for (int i = 1; i <= L; ++i) {
@@ -208,41 +289,66 @@ __device__ __noinline__ void shell_generic(Writer<NC>& w, double x, double y, do
     }
 }
 
+struct FusedArgs {
+  const NucleusEntry* nuclei;
+  const ShellEntry* shells;
+  const PrimEntry* prims;
+  const double* aof;
+  const NucleusChunk* chunks;
+  const ExpTable* exp_table;
+  const double* coord;      // [3][P]
+  const int32_t* perm;      // processing order of the points, or null
+  double* out;              // Vgl / Value
+  __nv_bfloat16* planes;    // Planes
+  int64_t point_num;
+  int64_t ao_num;
+  int64_t row_len;          // ao_num, or kp for Planes
+  int64_t task_num;
+  int chunk_num;
+};
+
 // One warp task: 32 points (lane = point) x one chunk of consecutive nuclei.
-template <int NC>
-__global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const NucleusEntry* __restrict__ nuclei,
-                                                               const ShellEntry* __restrict__ shells,
-                                                               const PrimEntry* __restrict__ prims,
-                                                               const double* __restrict__ aof,
-                                                               const NucleusChunk* __restrict__ chunks, int chunk_num,
-                                                               const double* __restrict__ coord, int64_t point_num,
-                                                               int64_t ao_num, int64_t task_num,
-                                                               double* __restrict__ out) {
+template <Out O>
+__global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a) {
+  constexpr int NC = ncomp<O>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* thi = reinterpret_cast<double*>(smem_raw);
+  double* tlo = thi + 32;
+  if constexpr (NC == 5 || O == Out::Value) {
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+      thi[i] = a.exp_table->hi[i];
+      tlo[i] = a.exp_table->lo[i];
+    }
+  }
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
-  if (task >= task_num) return;  // warp-uniform
-  const int64_t group = task / chunk_num;
-  const int ch = (int)(task - group * chunk_num);
+  if (task >= a.task_num) return;  // warp-uniform
+  const int64_t group = task / a.chunk_num;
+  const int ch = (int)(task - group * a.chunk_num);
   const int64_t p0 = group * 32;
-  const int64_t remaining = point_num - p0;
+  const int64_t remaining = a.point_num - p0;
   const int nvalid = remaining < 32 ? (int)remaining : 32;
-  const int64_t p = p0 + (lane < nvalid ? lane : nvalid - 1);
-  const double ex = coord[p], ey = coord[point_num + p], ez = coord[2 * point_num + p];
+  const int64_t slot = p0 + (lane < nvalid ? lane : nvalid - 1);
+  const int64_t p = a.perm ? (int64_t)a.perm[slot] : slot;
+  const int64_t P = a.point_num;
+  const double ex = a.coord[p], ey = a.coord[P + p], ez = a.coord[2 * P + p];
 
-  Writer<NC> w;
-  w.st = reinterpret_cast<Stage<NC>*>(smem_raw) + warp;
-  w.out = out;
-  w.p0 = p0;
-  w.ao_num = ao_num;
+  Writer<O> w;
+  w.st = reinterpret_cast<Stage<NC>*>(smem_raw + 512) + warp;
+  w.out = a.out;
+  w.planes = a.planes;
+  w.plane_stride = 5 * P * a.row_len;
+  w.row_len = a.row_len;
   w.nvalid = nvalid;
   w.lane = lane;
-  const NucleusChunk cj = chunks[ch];
+  w.st->pidx[lane] = p;
+  const NucleusChunk cj = a.chunks[ch];
   w.base = cj.ao_begin;
   w.fill = 0;
 
   for (int n = cj.nucl_begin; n < cj.nucl_end; ++n) {
-    const NucleusEntry& N = nuclei[n];
+    const NucleusEntry& N = a.nuclei[n];
     const double x = ex - N.x, y = ey - N.y, z = ez - N.z;
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
     const uint64_t r2b = bits_of(r2);
@@ -263,19 +369,19 @@ __global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const NucleusEntr
     Y[3] = Y[2] * y;
     Z[3] = Z[2] * z;
     for (int si = N.shell_begin; si < N.shell_end; ++si) {
-      const ShellEntry S = shells[si];
+      const ShellEntry S = a.shells[si];
       double t0 = 0.0, g = 0.0, h = 0.0;
       for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
-        const bool act = !scr && (r2b < __ldg(&prims[pi].thr_bits));
+        const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
         if (__any_sync(kFull, act)) {
-          const double expo = __ldg(&prims[pi].expo);
+          const double expo = __ldg(&a.prims[pi].expo);
           const double ar2 = expo * r2;
-          const double e = exp(-ar2);
-          double v = __ldg(&prims[pi].coef) * e;
+          const double e = exp_neg(ar2, thi, tlo);
+          double v = __ldg(&a.prims[pi].coef) * e;
           v = act ? v : 0.0;
           t0 += v;
           if constexpr (NC == 5) {
-            const double two_a = __ldg(&prims[pi].m2a) * v;
+            const double two_a = __ldg(&a.prims[pi].m2a) * v;
             g += two_a;
             h = fma(two_a, ar2, h);
           }
@@ -293,13 +399,17 @@ __global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const NucleusEntr
         sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
       }
       switch (S.l) {
-        case 0: shell_fixed<NC, 0>(w, X, Y, Z, sv, aof, S.ao_begin, scr); break;
-        case 1: shell_fixed<NC, 1>(w, X, Y, Z, sv, aof, S.ao_begin, scr); break;
-        case 2: shell_fixed<NC, 2>(w, X, Y, Z, sv, aof, S.ao_begin, scr); break;
-        case 3: shell_fixed<NC, 3>(w, X, Y, Z, sv, aof, S.ao_begin, scr); break;
-        default: shell_generic<NC>(w, x, y, z, S.l, sv, aof, S.ao_begin, scr); break;
+        case 0: shell_fixed<O, 0>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
+        case 1: shell_fixed<O, 1>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
+        case 2: shell_fixed<O, 2>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
+        case 3: shell_fixed<O, 3>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
+        default: shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr); break;
       }
     }
+  }
+  // BF16 planes are padded to a multiple of 64 columns; the last chunk zeroes the padding
+  if constexpr (O == Out::Planes) {
+    if (cj.ao_end == a.ao_num) w.emit_zeros((int)(a.row_len - a.ao_num));
   }
   w.flush();
 }
@@ -344,6 +454,60 @@ __global__ void shell_vgl_kernel(const NucleusEntry* __restrict__ nuclei, const 
   o[4 * shell_num] = t4;
 }
 
+// ---------------------------------------------------------------- point order
+// 15-bit Morton key of a point's cell on the 32^3 grid; one counter per cell.
+__global__ void morton_key_kernel(const double* __restrict__ coord, int64_t P, double ox, double oy, double oz,
+                                  double inv_cell, int32_t* __restrict__ keys, int32_t* __restrict__ counts) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const double c[3] = {(coord[p] - ox) * inv_cell, (coord[P + p] - oy) * inv_cell, (coord[2 * P + p] - oz) * inv_cell};
+  int key = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int q = c[d] > 0.0 ? (c[d] < 31.0 ? (int)c[d] : 31) : 0;  // NaN goes to cell 0
+#pragma unroll
+    for (int b = 0; b < 5; ++b) key |= ((q >> b) & 1) << (3 * b + d);
+  }
+  keys[p] = key;
+  atomicAdd(&counts[key], 1);
+}
+
+// In-place exclusive prefix sum of the kOrderCells counters, one CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) cell_scan_kernel(int32_t* __restrict__ counts) {
+  constexpr int kPer = kOrderCells / 1024;
+  __shared__ int32_t part[1024];
+  int32_t local[kPer];
+  int32_t s = 0;
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    local[i] = counts[t * kPer + i];
+    s += local[i];
+  }
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int32_t v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  int32_t run = part[t] - s;  // exclusive
+#pragma unroll
+  for (int i = 0; i < kPer; ++i) {
+    counts[t * kPer + i] = run;
+    run += local[i];
+  }
+}
+
+__global__ void cell_scatter_kernel(const int32_t* __restrict__ keys, int64_t P, int32_t* __restrict__ offsets,
+                                    int32_t* __restrict__ perm) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int pos = atomicAdd(&offsets[keys[p]], 1);
+  perm[pos] = (int32_t)p;
+}
+
 // Picks the nucleus-chunk level whose task count best fills the GPU.
 int pick_level(const AoTables& t, int64_t groups, int sms) {
   const int64_t target = (int64_t)sms * 16;  // ~16 warp tasks per SM
@@ -355,32 +519,72 @@ int pick_level(const AoTables& t, int64_t groups, int sms) {
   return best;
 }
 
-template <int NC>
-cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* out,
-                         const char* name) {
+template <Out O>
+cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
+                         double* out, __nv_bfloat16* planes, int64_t row_len, const char* name) {
   if (point_num <= 0 || t.ao_num <= 0) return cudaSuccess;
   const int64_t groups = (point_num + 31) / 32;
   const int lv = pick_level(t, groups, t.sm_count);
-  const int chunk_num = t.level_sizes[lv];
-  const NucleusChunk* chunks = t.chunks + t.level_offsets[lv];
-  const int64_t tasks = groups * chunk_num;
-  const int64_t blocks = (tasks + kWarps - 1) / kWarps;
-  const size_t smem = sizeof(Stage<NC>) * kWarps;
-  cudaFuncSetAttribute(ao_fused_kernel<NC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  FusedArgs a;
+  a.nuclei = t.nuclei;
+  a.shells = t.shells;
+  a.prims = t.prims;
+  a.aof = t.ao_factor;
+  a.chunk_num = t.level_sizes[lv];
+  a.chunks = t.chunks + t.level_offsets[lv];
+  a.exp_table = t.exp_table;
+  a.coord = coord;
+  a.perm = perm;
+  a.out = out;
+  a.planes = planes;
+  a.point_num = point_num;
+  a.ao_num = t.ao_num;
+  a.row_len = row_len;
+  a.task_num = groups * a.chunk_num;
+  const int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
+  const size_t smem = 512 + sizeof(Stage<ncomp<O>()>) * kWarps;
+  cudaFuncSetAttribute(ao_fused_kernel<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   LaunchScope scope(ctx, name);
-  ao_fused_kernel<NC><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(
-      t.nuclei, t.shells, t.prims, t.ao_factor, chunks, chunk_num, coord, point_num, t.ao_num, tasks, out);
+  ao_fused_kernel<O><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* ao_vgl) {
-  return launch_fused<5>(ctx, t, coord, point_num, ao_vgl, "ao_vgl_fused");
+cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int32_t* keys,
+                               int32_t* counts, int32_t* perm) {
+  if (point_num <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * kOrderCells, ctx->stream);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((point_num + 255) / 256);
+  {
+    LaunchScope scope(ctx, "point_order_keys");
+    morton_key_kernel<<<blocks, 256, 0, ctx->stream>>>(coord, point_num, t.grid_origin[0], t.grid_origin[1],
+                                                       t.grid_origin[2], t.grid_inv_cell, keys, counts);
+  }
+  {
+    LaunchScope scope(ctx, "point_order_scan");
+    cell_scan_kernel<<<1, 1024, 0, ctx->stream>>>(counts);
+  }
+  LaunchScope scope(ctx, "point_order_scatter");
+  cell_scatter_kernel<<<blocks, 256, 0, ctx->stream>>>(keys, point_num, counts, perm);
+  return cudaGetLastError();
 }
 
-cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* ao_value) {
-  return launch_fused<1>(ctx, t, coord, point_num, ao_value, "ao_value_fused");
+cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
+                          double* ao_vgl) {
+  return launch_fused<Out::Vgl>(ctx, t, coord, perm, point_num, ao_vgl, nullptr, t.ao_num, "ao_vgl_fused");
+}
+
+cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
+                            int64_t point_num, double* ao_value) {
+  return launch_fused<Out::Value>(ctx, t, coord, perm, point_num, ao_value, nullptr, t.ao_num, "ao_value_fused");
+}
+
+cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
+                             int64_t point_num, int64_t kp, void* planes) {
+  return launch_fused<Out::Planes>(ctx, t, coord, perm, point_num, nullptr, static_cast<__nv_bfloat16*>(planes), kp,
+                                   "ao_vgl_fused_bf16_planes");
 }
 
 cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int64_t shell_num,
@@ -392,6 +596,24 @@ cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, i
   LaunchScope scope(ctx, "shell_vgl");
   shell_vgl_kernel<<<(unsigned)((n + 127) / 128), 128, 0, ctx->stream>>>(
       t.nuclei, t.shells, t.prims, t.shell_orig, t.shell_nucl, coord, point_num, t.shell_num, shell_num, shell_vgl);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- exponential check
+namespace {
+__global__ void exp_check_kernel(const double* __restrict__ x, int64_t n, const ExpTable* __restrict__ tab,
+                                 double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[2 * i] = exp_neg(x[i], tab->hi, tab->lo);
+  out[2 * i + 1] = exp(-x[i]);
+}
+}  // namespace
+
+cudaError_t launch_exp_check(Ctx* ctx, const ExpTable* tab, const double* x, int64_t n, double* out) {
+  if (n <= 0) return cudaSuccess;
+  LaunchScope scope(ctx, "exp_check");
+  exp_check_kernel<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(x, n, tab, out);
   return cudaGetLastError();
 }
 

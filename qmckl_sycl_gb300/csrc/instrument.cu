@@ -89,6 +89,19 @@ qmckl_exit_code_device qmckl_host_unregister_device(qmckl_context_device context
   return QMCKL_SUCCESS_DEVICE;
 }
 
+qmckl_exit_code_device qmckl_exp_check_device(qmckl_context_device context, const double* x, int64_t n, double* out) {
+  if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
+  qg::Ctx* ctx = qg::ctx_of(context);
+  if (!ctx->ao_basis.provided)
+    return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, "qmckl_exp_check_device", nullptr);
+  qmckl_exit_code_device rc = qg::ensure_tables(ctx, context);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  if (!x || !out || n < 0)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, "qmckl_exp_check_device", "bad arguments");
+  qg::launch_exp_check(ctx, ctx->ao_basis.tables.exp_table, x, n, out);
+  return qg::finish(ctx, context, "qmckl_exp_check_device");
+}
+
 qmckl_exit_code_device qmckl_measure_fp64_peak_device(qmckl_context_device context, double* tflops) {
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (!tflops) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, "qmckl_measure_fp64_peak_device", "NULL");

@@ -55,6 +55,13 @@ struct NucleusChunk {
   int32_t ao_begin, ao_end;
 };
 
+// 2^(j/32), j = 0..31, as hi + lo doubles (hi = the double nearest to the value): the table of
+// the AO kernel's exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989).
+struct ExpTable {
+  double hi[32];
+  double lo[32];
+};
+
 struct AoTables {
   NucleusEntry* nuclei = nullptr;   // [nucl_num]
   ShellEntry* shells = nullptr;     // [shell_num] packed
@@ -66,6 +73,11 @@ struct AoTables {
   // Level v splits the nuclei into level_sizes[v] chunks of balanced cost, stored at
   // chunks + level_offsets[v]; the launch picks the level that fills the GPU.
   std::vector<int32_t> level_offsets, level_sizes;
+  ExpTable* exp_table = nullptr;    // device copy of the exponential's table
+  // grid for grouping points into spatially coherent warps: 32 cells per axis over the
+  // nuclei's bounding box plus a margin (points outside are clamped to the border cells)
+  double grid_origin[3] = {0, 0, 0};
+  double grid_inv_cell = 1.0;
   int32_t nucl_num = 0, shell_num = 0, prim_num = 0, ao_num = 0, lmax = 0;
   int sm_count = 152;
   bool valid = false;
@@ -132,6 +144,12 @@ struct AoBasisData {
   double* ao_value = nullptr;
   size_t ao_value_cap = 0;
   uint64_t ao_value_date = 0;
+  // processing order of the current points (see launch_point_order), valid for perm_date
+  int32_t* point_perm = nullptr;
+  int32_t* point_keys = nullptr;
+  int32_t* cell_counts = nullptr;
+  size_t perm_cap = 0, keys_cap = 0, counts_cap = 0;
+  uint64_t perm_date = 0;
   int32_t uninitialized = 0;
   bool provided = false;
 };
@@ -226,6 +244,12 @@ void dfree(Ctx* ctx, void* p);
 bool ensure(Ctx* ctx, double** buf, size_t* cap, size_t bytes);
 bool ensure_raw(Ctx* ctx, void** buf, size_t* cap, size_t bytes);
 
+// AO kernel tables (built on first use after finalize) and the processing order of the
+// current points (null: identity order), both in ao_basis.cpp.
+qmckl_exit_code_device ensure_tables(Ctx* ctx, qmckl_context_device c);
+const int32_t* point_order(Ctx* ctx);
+cudaError_t launch_exp_check(Ctx* ctx, const ExpTable* tab, const double* x, int64_t n, double* out);
+
 // Selects the context's device and creates its stream on first use.
 bool ensure_device(Ctx* ctx);
 // True when a kernel may dereference p (device, managed or page-locked host memory).
@@ -248,8 +272,21 @@ struct LaunchScope {
 };
 
 // ---- kernel entry points (ao_kernels.cu, mo_kernels.cu, util_kernels.cu) ----
-cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* ao_vgl);
-cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, double* ao_value);
+// Number of grid cells used by launch_point_order (32 per axis).
+constexpr int kOrderCells = 32 * 32 * 32;
+// perm <- an order of the points that puts spatial neighbours in the same warp (counting
+// sort of their Morton cell keys); keys [P] and counts [kOrderCells] are scratch.
+cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int32_t* keys,
+                               int32_t* counts, int32_t* perm);
+// Fused AO kernels; perm (may be null) is the processing order of the points.
+cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
+                          double* ao_vgl);
+cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
+                            int64_t point_num, double* ao_value);
+// AO vgl written straight as the three BF16 planes of the split-BF16 contraction, planes
+// [3][5P][kp] (columns [ao_num, kp) zero), with the reference's zero-value skip applied.
+cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
+                             int64_t point_num, int64_t kp, void* planes);
 cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num,
                              int64_t shell_num, double* shell_vgl);
 // mo_vgl[5P][M] = ao_vgl[5P][A] * coef_t[A][M], skipping (for components 1..4) the AOs whose

@@ -140,9 +140,11 @@ bool qmckl_mo_basis_select_mo_device(qmckl_context_device context, int32_t* keep
 // ---------------------------------------------------------------- provides
 static qmckl_exit_code_device compute_mo_vgl(Ctx* ctx, qmckl_context_device context, double* dst) {
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
+  if (!ctx->ao_basis.provided) return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, "qmckl_ao_basis", nullptr);
+  // the split-BF16 form takes the AO operand straight from the fused AO kernel
+  if (ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE) return provide_mo_split(ctx, context, dst, false);
   qmckl_exit_code_device rc = qmckl_provide_ao_basis_ao_vgl_device(context);
   if (rc != QMCKL_SUCCESS_DEVICE) return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, "qmckl_ao_basis", nullptr);
-  if (ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE) return provide_mo_split(ctx, context, dst, false);
   launch_mo_vgl_fp64(ctx, ctx->ao_basis.ao_vgl, ctx->mo_basis.coefficient_t, ctx->point.num, ctx->ao_basis.ao_num,
                      ctx->mo_basis.mo_num, dst);
   return finish(ctx, context, fn);

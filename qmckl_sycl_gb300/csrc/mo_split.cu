@@ -475,27 +475,12 @@ static qmckl_exit_code_device ensure_coef_planes(Ctx* ctx, qmckl_context_device 
   return finish(ctx, c, "qmckl_provide_mo_basis_mo_vgl_device");
 }
 
-// out[rows][M] = split-BF16 product of src[rows][A] (FP64, ld = A) and the coefficients.
-qmckl_exit_code_device split_contract(Ctx* ctx, qmckl_context_device c, const double* src, int64_t rows, bool mask5,
-                                      double* out) {
+// out[rows][M] = split-BF16 product of the A planes ap ([3][rows][kp]) and the coefficients.
+static qmckl_exit_code_device contract_planes(Ctx* ctx, qmckl_context_device c, const __nv_bfloat16* ap, int64_t rows,
+                                              int64_t kp, int* err, double* out, const char* name) {
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
   MoBasisData& mo = ctx->mo_basis;
-  const int64_t A = ctx->ao_basis.ao_num, M = mo.mo_num;
-  if (rows <= 0 || M <= 0) return QMCKL_SUCCESS_DEVICE;
-  const int64_t kp = round_up(A, kBK);
-  if (kp / kBK > (int64_t)INT32_MAX || rows > (int64_t)INT32_MAX - kBM)
-    return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
-  qmckl_exit_code_device rc = ensure_coef_planes(ctx, c, kp);
-  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
-  const size_t need = sizeof(__nv_bfloat16) * 3 * (size_t)rows * (size_t)kp + 256;
-  if (!ensure_raw(ctx, &mo.ao_split, &mo.ao_split_cap, need))
-    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
-  __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
-  // error word lives after the planes
-  int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(mo.ao_split) + need - 256);
-  launch_split(ctx, src, rows, A, A, kp, mask5, ap);
-  cudaMemsetAsync(err, 0, sizeof(int), ctx->stream);
-
+  const int64_t M = mo.mo_num;
   const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
   const int n_tile = (int)round_up((M + ntiles - 1) / ntiles, 16);
   uint32_t tcols = 32;
@@ -520,10 +505,10 @@ qmckl_exit_code_device split_contract(Ctx* ctx, qmckl_context_device c, const do
   cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid((unsigned)((rows + kBM - 1) / kBM), (unsigned)ntiles);
   {
-    LaunchScope scope(ctx, mask5 ? "mo_vgl_split_bf16" : "mo_value_split_bf16");
+    LaunchScope scope(ctx, name);
     split_gemm_kernel<<<grid, kThreads, smem, ctx->stream>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], args);
   }
-  rc = finish(ctx, c, fn);
+  qmckl_exit_code_device rc = finish(ctx, c, fn);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
   if (!ctx->async) {
     int h = 0;
@@ -533,10 +518,57 @@ qmckl_exit_code_device split_contract(Ctx* ctx, qmckl_context_device c, const do
   return QMCKL_SUCCESS_DEVICE;
 }
 
+// Ensures the A-plane buffer holds rows x kp planes plus the error word; returns the error word.
+static int* ensure_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
+  MoBasisData& mo = ctx->mo_basis;
+  const size_t need = sizeof(__nv_bfloat16) * 3 * (size_t)rows * (size_t)kp + 256;
+  if (!ensure_raw(ctx, &mo.ao_split, &mo.ao_split_cap, need)) return nullptr;
+  int* err = reinterpret_cast<int*>(reinterpret_cast<char*>(mo.ao_split) + need - 256);
+  cudaMemsetAsync(err, 0, sizeof(int), ctx->stream);
+  return err;
+}
+
+// out[rows][M] = split-BF16 product of src[rows][A] (FP64, ld = A) and the coefficients.
+qmckl_exit_code_device split_contract(Ctx* ctx, qmckl_context_device c, const double* src, int64_t rows, bool mask5,
+                                      double* out) {
+  const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
+  MoBasisData& mo = ctx->mo_basis;
+  const int64_t A = ctx->ao_basis.ao_num, M = mo.mo_num;
+  if (rows <= 0 || M <= 0) return QMCKL_SUCCESS_DEVICE;
+  const int64_t kp = round_up(A, kBK);
+  if (kp / kBK > (int64_t)INT32_MAX || rows > (int64_t)INT32_MAX - kBM)
+    return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
+  qmckl_exit_code_device rc = ensure_coef_planes(ctx, c, kp);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  int* err = ensure_a_planes(ctx, rows, kp);
+  if (!err) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
+  __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
+  launch_split(ctx, src, rows, A, A, kp, mask5, ap);
+  return contract_planes(ctx, c, ap, rows, kp, err, out, mask5 ? "mo_vgl_split_bf16" : "mo_value_split_bf16");
+}
+
+// mo_vgl for the current points: the fused AO kernel writes the BF16 planes of the AO
+// operand directly (no FP64 ao_vgl round trip), then the tensor-core contraction.
+static qmckl_exit_code_device split_mo_vgl(Ctx* ctx, qmckl_context_device c, double* out) {
+  const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
+  const int64_t P = ctx->point.num, A = ctx->ao_basis.ao_num, M = ctx->mo_basis.mo_num;
+  if (P <= 0 || M <= 0) return QMCKL_SUCCESS_DEVICE;
+  const int64_t rows = 5 * P, kp = round_up(A, kBK);
+  if (rows > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
+  qmckl_exit_code_device rc = ensure_tables(ctx, c);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  rc = ensure_coef_planes(ctx, c, kp);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  int* err = ensure_a_planes(ctx, rows, kp);
+  if (!err) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
+  __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(ctx->mo_basis.ao_split);
+  launch_ao_planes(ctx, ctx->ao_basis.tables, ctx->point.coord, point_order(ctx), P, kp, ap);
+  return contract_planes(ctx, c, ap, rows, kp, err, out, "mo_vgl_split_bf16");
+}
+
 qmckl_exit_code_device provide_mo_split(Ctx* ctx, qmckl_context_device c, double* dst, bool value_only) {
-  if (value_only)
-    return split_contract(ctx, c, ctx->ao_basis.ao_value, ctx->point.num, false, dst);
-  return split_contract(ctx, c, ctx->ao_basis.ao_vgl, 5 * ctx->point.num, true, dst);
+  if (value_only) return split_contract(ctx, c, ctx->ao_basis.ao_value, ctx->point.num, false, dst);
+  return split_mo_vgl(ctx, c, dst);
 }
 
 }  // namespace qg

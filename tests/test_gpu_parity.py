@@ -240,3 +240,42 @@ def test_empty_point_set(chbrclf):
         ctx.call("set_point", b"N", 0, dummy.ctypes.data_as(ctypes.c_void_p), 0)
         out = np.zeros(1)
         ctx.call("get_mo_basis_mo_vgl", out.ctypes.data_as(ctypes.c_void_p), 0)
+
+
+def _ulps(a, b):
+    # distance in units in the last place, for positive doubles (integer arithmetic on the
+    # bit patterns: a float64 cast of ~2^62-sized integers would round to multiples of 512)
+    return np.abs(np.ascontiguousarray(a).view(np.int64) - np.ascontiguousarray(b).view(np.int64))
+
+
+def test_kernel_exponential_against_cuda_and_libm(chbrclf):
+    # the fused AO kernel's table-driven e^-x on the screened range [0, 27.7]
+    rng = np.random.default_rng(0)
+    x = np.concatenate([rng.uniform(0.0, 27.7, 1 << 20), np.linspace(0.0, 27.7, 4097), [0.0, 1e-300, 27.631021115928547]])
+    with Context(0) as ctx:
+        ctx.load_system(chbrclf, mo=False, points=False)
+        dx = ctx.upload(x)
+        out = ctx.buffer("exp_out", 16 * x.size)
+        ctx.call("exp_check", ctypes.c_void_p(dx.ptr), x.size, ctypes.c_void_p(out.ptr))
+        got = ctx.download(out.ptr, (x.size, 2))
+    ours, cuda = got[:, 0], got[:, 1]
+    libm = np.exp(-x)
+    for name, other in (("cuda", cuda), ("libm", libm)):
+        u = _ulps(ours, other)
+        bad = np.argsort(u)[-5:]
+        print("vs %s: max %d ulp; worst x %s ours %s other %s" % (
+            name, u.max(), x[bad].tolist(), ours[bad].tolist(), other[bad].tolist()))
+        print("   cuda vs libm at those x:", _ulps(cuda[bad], libm[bad]).tolist())
+    assert _ulps(ours, cuda).max() <= 2
+    assert _ulps(ours, libm).max() <= 2
+    assert ours[x.size - 3] == 1.0
+
+
+def test_point_order_does_not_change_results():
+    # results depend only on each point, not on which points share a warp
+    s = config_small(11, point_num=300)
+    perm = np.random.default_rng(1).permutation(s.point_num)
+    a = run_all(s)
+    b = run_all(s.with_points(s.coord[perm]))
+    for k in a:
+        assert np.array_equal(a[k][perm], b[k]), k
