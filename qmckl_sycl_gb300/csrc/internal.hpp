@@ -170,6 +170,8 @@ struct MoBasisData {
   int64_t split_mo_pad = 0, split_ao_pad = 0;
   void* ao_split = nullptr;
   size_t ao_split_cap = 0;
+  void* split_job = nullptr;  // device copy of the contraction's job descriptor
+  size_t split_job_cap = 0;
   int32_t uninitialized = 0;
   bool provided = false;
 };

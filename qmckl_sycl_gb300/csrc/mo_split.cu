@@ -180,15 +180,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-struct TileArgs {
-  double* out;       // [rows][ldo]
-  int64_t rows;      // valid rows
-  int64_t cols;      // valid columns (MO count)
+// One contraction (one molecule): its six operand tensor maps and output. Jobs live in
+// global memory so that one persistent launch can work through the tiles of many of them;
+// tile t of the launch belongs to the job with the largest tile_begin <= t.
+struct alignas(64) SplitJob {
+  CUtensorMap ta[3];  // A planes [3][rows][kp]
+  CUtensorMap tb[3];  // B planes [3][cols][kp]
+  double* out;        // [rows][ldo]
+  int64_t rows;       // valid rows
+  int64_t cols;       // valid columns (MO count)
   int64_t ldo;
-  int kblocks;       // Kp / 64
-  int n_tile;        // columns per tile (multiple of 16, <= kMaxN)
-  uint32_t tmem_cols;
-  int* error;        // set to a non-zero code on a wait timeout
+  int32_t kblocks;    // kp / 64
+  int32_t n_tile;     // columns per tile (multiple of 16, <= kMaxN)
+  int32_t col_tiles;  // tiles along the columns
+  int32_t tile_begin; // index of this job's first tile in the launch
 };
 
 // Correction terms (A plane, B plane): hi*mid, mid*hi, hi*lo, mid*mid, lo*hi.
@@ -233,180 +238,198 @@ __device__ __forceinline__ void set_abort(volatile int* abort_flag, int* error, 
 // Tensor-memory columns: [0,N) corrections, [N,2N) and [2N,3N) main product ping-pong
 // buffers (one 64-wide K block each), [3N,4N) and [4N,5N) the running FP32 two-sum (hi, lo)
 // of the main product, folded in by the epilogue warps after every K block.
+//
+// Persistent: CTA b processes tiles b, b + gridDim.x, ... of the launch (tiles of one job
+// are ordered column tile fastest, so CTAs running at the same time share A rows in L2).
+// Tensor memory (512 columns) is allocated once; the barriers are re-initialised per tile.
 __global__ void __launch_bounds__(kThreads, 1)
-    split_gemm_kernel(const __grid_constant__ CUtensorMap ta0, const __grid_constant__ CUtensorMap ta1,
-                      const __grid_constant__ CUtensorMap ta2, const __grid_constant__ CUtensorMap tb0,
-                      const __grid_constant__ CUtensorMap tb1, const __grid_constant__ CUtensorMap tb2, TileArgs p) {
+    split_gemm_kernel(const SplitJob* __restrict__ jobs, int njobs, int total_tiles, int* error) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const uint32_t plane_b = (uint32_t)p.n_tile * kBK * 2;
-  const uint32_t stage_bytes = 3 * kPlaneA + 3 * plane_b;
-  uint64_t* full = (uint64_t*)(base + kStages * stage_bytes);
+  const uint32_t max_stage = 3 * kPlaneA + 3 * (uint32_t)kMaxN * kBK * 2;
+  uint64_t* full = (uint64_t*)(base + kStages * max_stage);
   uint64_t* empty = full + kStages;
   uint64_t* accf = empty + kStages;  // [2] main buffer filled (MMA -> epilogue)
   uint64_t* acce = accf + 2;         // [2] main buffer folded (epilogue -> MMA)
   uint64_t* mma_done = acce + 2;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  const uint32_t tmem_cols = 512;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kBM;
-  const int n0 = blockIdx.y * p.n_tile;
-  const int N = p.n_tile;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
-    }
-    mbar_init(mma_done, 1);
-    *abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(p.tmem_cols));
+                 "r"(tmem_cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
+  if (threadIdx.x == 0) *abort_flag = 0;
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (warp == 0) {
-    if (lane == 0) {
-      const CUtensorMap* ta[3] = {&ta0, &ta1, &ta2};
-      const CUtensorMap* tb[3] = {&tb0, &tb1, &tb2};
-      int issued = 0;
-      bool ok = true;
-      for (int kb = 0; kb < p.kblocks; ++kb) {
-        const int s = kb % kStages;
-        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-        if (!wait_or_abort(&empty[s], ph ^ 1u, abort_flag)) {
-          ok = false;
-          set_abort(abort_flag, p.error, 1);
-          break;
-        }
-        unsigned char* st = base + s * stage_bytes;
-        mbar_expect_tx(&full[s], stage_bytes);
-        for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, ta[i], kb * kBK, m0, &full[s]);
-        for (int i = 0; i < 3; ++i) tma_load_2d(st + 3 * kPlaneA + i * plane_b, tb[i], kb * kBK, n0, &full[s]);
-        issued = kb + 1;
+  int done_phases = 0;  // mma_done completions so far (one per tile with MMAs issued)
+  for (int tile = blockIdx.x; tile < total_tiles && !*abort_flag; tile += gridDim.x) {
+    int j = 0;
+    while (j + 1 < njobs && jobs[j + 1].tile_begin <= tile) ++j;
+    const SplitJob& job = jobs[j];
+    const int local = tile - job.tile_begin;
+    const int N = job.n_tile;
+    const int m0 = (local / job.col_tiles) * kBM;
+    const int n0 = (local % job.col_tiles) * N;
+    const uint32_t plane_b = (uint32_t)N * kBK * 2;
+    const uint32_t stage_bytes = 3 * kPlaneA + 3 * plane_b;
+
+    if (threadIdx.x == 0) {
+      for (int s2 = 0; s2 < kStages; ++s2) {
+        mbar_init(&full[s2], 1);
+        mbar_init(&empty[s2], 1);
       }
-      if (!ok) {
-        // drain the loads still in flight before the CTA's shared memory is released
-        for (int kb = issued - kStages < 0 ? 0 : issued - kStages; kb < issued; ++kb)
-          mbar_wait(&full[kb % kStages], (uint32_t)(kb / kStages) & 1u);
+      for (int b = 0; b < 2; ++b) {
+        mbar_init(&accf[b], 1);
+        mbar_init(&acce[b], 4);
       }
+      mbar_init(mma_done, 1);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-  } else if (warp == 1) {
-    if (lane == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-                             ((uint32_t)(kBM >> 4) << 24);
-      for (int kb = 0; kb < p.kblocks; ++kb) {
-        const int s = kb % kStages, b = kb & 1, use = kb >> 1;
-        const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-        if (use > 0 && !wait_or_abort(&acce[b], (uint32_t)(use - 1) & 1u, abort_flag)) {
-          set_abort(abort_flag, p.error, 2);
-          break;
+    __syncthreads();
+
+    if (warp == 0) {
+      if (lane == 0) {
+        for (int i = 0; i < 3; ++i) {
+          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((uint64_t)&job.ta[i]) : "memory");
+          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((uint64_t)&job.tb[i]) : "memory");
         }
-        if (!wait_or_abort(&full[s], ph, abort_flag)) {
-          set_abort(abort_flag, p.error, 3);
+        int issued = 0;
+        bool ok = true;
+        for (int kb = 0; kb < job.kblocks; ++kb) {
+          const int s2 = kb % kStages;
+          const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+          if (!wait_or_abort(&empty[s2], ph ^ 1u, abort_flag)) {
+            ok = false;
+            set_abort(abort_flag, error, 1);
+            break;
+          }
+          unsigned char* st = base + s2 * stage_bytes;
+          mbar_expect_tx(&full[s2], stage_bytes);
+          for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, &job.ta[i], kb * kBK, m0, &full[s2]);
+          for (int i = 0; i < 3; ++i) tma_load_2d(st + 3 * kPlaneA + i * plane_b, &job.tb[i], kb * kBK, n0, &full[s2]);
+          issued = kb + 1;
+        }
+        if (!ok) {
+          // drain the loads still in flight before the shared memory is reused or released
+          for (int kb = issued - kStages < 0 ? 0 : issued - kStages; kb < issued; ++kb)
+            mbar_wait(&full[kb % kStages], (uint32_t)(kb / kStages) & 1u);
+        }
+      }
+    } else if (warp == 1) {
+      if (lane == 0) {
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+                               ((uint32_t)(kBM >> 4) << 24);
+        for (int kb = 0; kb < job.kblocks; ++kb) {
+          const int s2 = kb % kStages, b = kb & 1, use = kb >> 1;
+          const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+          if (use > 0 && !wait_or_abort(&acce[b], (uint32_t)(use - 1) & 1u, abort_flag)) {
+            set_abort(abort_flag, error, 2);
+            break;
+          }
+          if (!wait_or_abort(&full[s2], ph, abort_flag)) {
+            set_abort(abort_flag, error, 3);
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(base + s2 * stage_bytes);
+          const uint32_t sb = sa + 3 * kPlaneA;
+          const uint32_t main_acc = tmem + (uint32_t)((1 + b) * N);
+#pragma unroll
+          for (int kk = 0; kk < kBK / 16; ++kk) {
+            umma_bf16(main_acc, sdesc(sa + kk * 32), sdesc(sb + kk * 32), idesc, kk > 0 ? 1u : 0u);
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+              const uint64_t ad = sdesc(sa + kPairA[t] * kPlaneA + kk * 32);
+              const uint64_t bd = sdesc(sb + kPairB[t] * plane_b + kk * 32);
+              umma_bf16(tmem, ad, bd, idesc, (kb | kk | t) != 0);
+            }
+          }
+          umma_commit(&empty[s2]);  // frees the stage once these MMAs have read it
+          umma_commit(&accf[b]);    // main buffer b holds this block's product
+        }
+        umma_commit(mma_done);  // every MMA of this tile has completed
+      }
+    } else {
+      // epilogue: warp w owns TMEM lanes 32*(w % 4) .. +31 (one output row per thread)
+      const int quarter = warp & 3;
+      const int64_t row = (int64_t)m0 + quarter * 32 + lane;
+      const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
+      const uint32_t hi_col = 3 * N, lo_col = 4 * N;
+      bool ok = true;
+      for (int kb = 0; kb < job.kblocks; ++kb) {
+        const int b = kb & 1, use = kb >> 1;
+        if (!wait_or_abort(&accf[b], (uint32_t)use & 1u, abort_flag)) {
+          set_abort(abort_flag, error, 4);
+          ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t sa = smem_u32(base + s * stage_bytes);
-        const uint32_t sb = sa + 3 * kPlaneA;
-        const uint32_t main_acc = tmem + (uint32_t)((1 + b) * N);
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          float v[16], hi[16], lo[16];
+          tmem_ld16(lb + (uint32_t)((1 + b) * N + c0), v);
+          if (kb == 0) {
 #pragma unroll
-        for (int kk = 0; kk < kBK / 16; ++kk) {
-          umma_bf16(main_acc, sdesc(sa + kk * 32), sdesc(sb + kk * 32), idesc, kk > 0 ? 1u : 0u);
+            for (int q = 0; q < 16; ++q) {
+              hi[q] = v[q];
+              lo[q] = 0.f;
+            }
+          } else {
+            tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
+            tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
 #pragma unroll
-          for (int t = 0; t < 5; ++t) {
-            const uint64_t ad = sdesc(sa + kPairA[t] * kPlaneA + kk * 32);
-            const uint64_t bd = sdesc(sb + kPairB[t] * plane_b + kk * 32);
-            umma_bf16(tmem, ad, bd, idesc, (kb | kk | t) != 0);
+            for (int q = 0; q < 16; ++q) {
+              float s2, e2;
+              two_sum(hi[q], v[q], s2, e2);
+              hi[q] = s2;
+              lo[q] += e2;
+            }
           }
+          tmem_st16(lb + hi_col + (uint32_t)c0, hi);
+          tmem_st16(lb + lo_col + (uint32_t)c0, lo);
         }
-        umma_commit(&empty[s]);  // frees the stage once these MMAs have read it
-        umma_commit(&accf[b]);   // main buffer b holds this block's product
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[b]);
       }
-      umma_commit(mma_done);  // every MMA this thread issued has completed
-    }
-  } else {
-    // epilogue: warp w owns TMEM lanes 32*(w % 4) .. +31 (one output row per thread)
-    const int quarter = warp & 3;
-    const int64_t row = (int64_t)m0 + quarter * 32 + lane;
-    const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
-    const uint32_t hi_col = 3 * N, lo_col = 4 * N;
-    bool ok = true;
-    for (int kb = 0; kb < p.kblocks; ++kb) {
-      const int b = kb & 1, use = kb >> 1;
-      if (!wait_or_abort(&accf[b], (uint32_t)use & 1u, abort_flag)) {
-        set_abort(abort_flag, p.error, 4);
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float v[16], hi[16], lo[16];
-        tmem_ld16(lb + (uint32_t)((1 + b) * N + c0), v);
-        if (kb == 0) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            hi[j] = v[j];
-            lo[j] = 0.f;
-          }
-        } else {
+      if (ok) {
+        // the last accf phase covered every MMA of the tile, corrections included
+        for (int c0 = 0; c0 < N; c0 += 16) {
+          float c[16], hi[16], lo[16];
+          tmem_ld16(lb + (uint32_t)c0, c);
           tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
           tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
+          if (row < job.rows) {
+            double* o = job.out + row * job.ldo + n0 + c0;
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            float s2, e2;
-            two_sum(hi[j], v[j], s2, e2);
-            hi[j] = s2;
-            lo[j] += e2;
-          }
-        }
-        tmem_st16(lb + hi_col + (uint32_t)c0, hi);
-        tmem_st16(lb + lo_col + (uint32_t)c0, lo);
-      }
-      asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acce[b]);
-    }
-    if (ok) {
-      // the last accf phase covered every MMA, corrections included
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float c[16], hi[16], lo[16];
-        tmem_ld16(lb + (uint32_t)c0, c);
-        tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
-        tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
-        if (row < p.rows) {
-          double* o = p.out + row * p.ldo + n0 + c0;
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            float s2, e2;
-            two_sum(hi[j], c[j], s2, e2);
-            if (n0 + c0 + j < p.cols) o[j] = f32_to_f64_int(s2) + f32_to_f64_int(lo[j] + e2);
+            for (int q = 0; q < 16; ++q) {
+              float s2, e2;
+              two_sum(hi[q], c[q], s2, e2);
+              if (n0 + c0 + q < job.cols) o[q] = f32_to_f64_int(s2) + f32_to_f64_int(lo[q] + e2);
+            }
           }
         }
       }
     }
+    // no MMA of this tile may still run when its barriers and tensor memory are reused
+    if (warp == 1 && lane == 0) mbar_wait(mma_done, 0);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    ++done_phases;
   }
-  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  (void)done_phases;
   __syncthreads();
   if (warp == 1) {
-    // no MMA may still be writing tensor memory when it is released
-    if (lane == 0) mbar_wait(mma_done, 0);
-    __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(p.tmem_cols));
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols));
   }
 }
 
@@ -448,6 +471,49 @@ bool encode_map(CUtensorMap* map, const void* base, int64_t rows, int64_t kp, in
 
 int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
+// Column tiling of an M-column contraction: the fewest tiles of at most kMaxN columns,
+// as equal as multiples of 16 allow.
+int tile_cols(int64_t M) {
+  const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
+  return (int)round_up((M + ntiles - 1) / ntiles, 16);
+}
+
+// Describes out[rows][M] = A planes (ap, [3][rows][kp]) x B planes (bp, [3][M][kp])^T as a
+// job whose tiles start at tile_begin; returns its tile count, or -1 if a map fails.
+int make_job(SplitJob& job, const __nv_bfloat16* ap, int64_t rows, const __nv_bfloat16* bp, int64_t M, int64_t kp,
+             double* out, int tile_begin) {
+  memset(&job, 0, sizeof job);
+  const int n_tile = tile_cols(M);
+  for (int i = 0; i < 3; ++i)
+    if (!encode_map(&job.ta[i], ap + (size_t)i * rows * kp, rows, kp, kBM) ||
+        !encode_map(&job.tb[i], bp + (size_t)i * M * kp, M, kp, n_tile))
+      return -1;
+  job.out = out;
+  job.rows = rows;
+  job.cols = M;
+  job.ldo = M;
+  job.kblocks = (int32_t)(kp / kBK);
+  job.n_tile = n_tile;
+  job.col_tiles = (int32_t)((M + n_tile - 1) / n_tile);
+  job.tile_begin = tile_begin;
+  return (int)((rows + kBM - 1) / kBM) * job.col_tiles;
+}
+
+size_t split_smem_bytes() { return 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)kMaxN * kBK * 2) + 256; }
+
+// One persistent launch over every tile of the njobs jobs at d_jobs (device memory).
+cudaError_t launch_split_jobs(cudaStream_t stream, const SplitJob* d_jobs, int njobs, int total_tiles, int* err) {
+  if (total_tiles <= 0) return cudaSuccess;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t smem = split_smem_bytes();
+  cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int grid = total_tiles < sms ? total_tiles : sms;
+  split_gemm_kernel<<<grid, kThreads, smem, stream>>>(d_jobs, njobs, total_tiles, err);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_split(Ctx* ctx, const double* src, int64_t rows, int64_t k, int64_t ld, int64_t kp, bool mask5,
                          __nv_bfloat16* planes) {
   const int64_t n = rows * kp;
@@ -480,33 +546,19 @@ static qmckl_exit_code_device contract_planes(Ctx* ctx, qmckl_context_device c, 
                                               int64_t kp, int* err, double* out, const char* name) {
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
   MoBasisData& mo = ctx->mo_basis;
-  const int64_t M = mo.mo_num;
-  const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
-  const int n_tile = (int)round_up((M + ntiles - 1) / ntiles, 16);
-  uint32_t tcols = 32;
-  while ((int)tcols < 5 * n_tile) tcols *= 2;
-  CUtensorMap ta[3], tb[3];
-  const __nv_bfloat16* bp = static_cast<const __nv_bfloat16*>(mo.coef_split);
-  for (int i = 0; i < 3; ++i) {
-    if (!encode_map(&ta[i], ap + (size_t)i * rows * kp, rows, kp, kBM) ||
-        !encode_map(&tb[i], bp + (size_t)i * M * kp, M, kp, n_tile))
-      return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
+  SplitJob job;
+  const int tiles =
+      make_job(job, ap, rows, static_cast<const __nv_bfloat16*>(mo.coef_split), mo.mo_num, kp, out, 0);
+  if (tiles < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
+  if (!ensure_raw(ctx, &mo.split_job, &mo.split_job_cap, sizeof(SplitJob)))
+    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptor");
+  if (cudaMemcpyAsync(mo.split_job, &job, sizeof job, cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, QMCKL_FAILURE_DEVICE, fn, "job upload failed");
   }
-  TileArgs args;
-  args.out = out;
-  args.rows = rows;
-  args.cols = M;
-  args.ldo = M;
-  args.kblocks = (int)(kp / kBK);
-  args.n_tile = n_tile;
-  args.tmem_cols = tcols;
-  args.error = err;
-  const size_t smem = 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)n_tile * kBK * 2) + 256;
-  cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  dim3 grid((unsigned)((rows + kBM - 1) / kBM), (unsigned)ntiles);
   {
     LaunchScope scope(ctx, name);
-    split_gemm_kernel<<<grid, kThreads, smem, ctx->stream>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], args);
+    launch_split_jobs(ctx->stream, static_cast<const SplitJob*>(mo.split_job), 1, tiles, err);
   }
   qmckl_exit_code_device rc = finish(ctx, c, fn);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -593,7 +645,7 @@ constexpr int64_t kNoAllocMaxAo = 2048;
 constexpr int64_t kNoAllocMaxMo = 1024;
 constexpr int64_t kNoAllocChunkRows = 1280;  // a multiple of 128 (tile rows) and of 5 (vgl rows of a point)
 constexpr size_t kNoAllocBytes =
-    sizeof(__nv_bfloat16) * 3 * (size_t)(kNoAllocMaxMo + kNoAllocChunkRows) * (size_t)kNoAllocMaxAo + 256;
+    sizeof(__nv_bfloat16) * 3 * (size_t)(kNoAllocMaxMo + kNoAllocChunkRows) * (size_t)kNoAllocMaxAo + 2048;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
@@ -652,12 +704,7 @@ extern "C" qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(co
     return QMCKL_FAILURE_DEVICE;
   }
 
-  const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
-  const int n_tile = (int)round_up((M + ntiles - 1) / ntiles, 16);
-  uint32_t tcols = 32;
-  while ((int)tcols < 5 * n_tile) tcols *= 2;
-  const size_t smem = 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)n_tile * kBK * 2) + 256;
-  cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  SplitJob* djob = reinterpret_cast<SplitJob*>(static_cast<unsigned char*>(scratch) + kNoAllocBytes - 2048);
 
   auto split = [&](const double* src, int64_t n, int64_t ld, bool mask, __nv_bfloat16* dst) {
     int64_t blocks = (n * kp + 255) / 256;
@@ -665,27 +712,19 @@ extern "C" qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(co
     split_planes_kernel<<<(unsigned)blocks, 256, 0, stream>>>(src, n, ao_num, ld, kp, mask ? 1 : 0, dst);
   };
   split(coefficient, M, ao_num, false, bplanes);
-  CUtensorMap tb[3];
-  for (int i = 0; i < 3; ++i)
-    if (!encode_map(&tb[i], bplanes + (size_t)i * M * kp, M, kp, n_tile)) return QMCKL_FAILURE_DEVICE;
 
   for (int64_t r0 = 0; r0 < rows; r0 += kNoAllocChunkRows) {
     const int64_t n = rows - r0 < kNoAllocChunkRows ? rows - r0 : kNoAllocChunkRows;
     split(ao + r0 * ao_num, n, ao_num, vgl_mask != 0, aplanes);
-    CUtensorMap ta[3];
-    for (int i = 0; i < 3; ++i)
-      if (!encode_map(&ta[i], aplanes + (size_t)i * n * kp, n, kp, kBM)) return QMCKL_FAILURE_DEVICE;
-    TileArgs args;
-    args.out = out + r0 * M;
-    args.rows = n;
-    args.cols = M;
-    args.ldo = M;
-    args.kblocks = (int)(kp / kBK);
-    args.n_tile = n_tile;
-    args.tmem_cols = tcols;
-    args.error = err;
-    dim3 grid((unsigned)((n + kBM - 1) / kBM), (unsigned)ntiles);
-    split_gemm_kernel<<<grid, kThreads, smem, stream>>>(ta[0], ta[1], ta[2], tb[0], tb[1], tb[2], args);
+    SplitJob job;
+    const int tiles = make_job(job, aplanes, n, bplanes, M, kp, out + r0 * M, 0);
+    if (tiles < 0) return QMCKL_FAILURE_DEVICE;
+    // the descriptor lives in the array too; the copy is ordered after the previous chunk's kernel
+    if (cudaMemcpyAsync(djob, &job, sizeof job, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+      cudaGetLastError();
+      return QMCKL_FAILURE_DEVICE;
+    }
+    launch_split_jobs(stream, djob, 1, tiles, err);
   }
   int h = 0;
   if (cudaGetLastError() != cudaSuccess ||
