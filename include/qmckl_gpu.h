@@ -358,6 +358,49 @@ qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(const double*
                                                                    const double* coefficient, int64_t mo_num,
                                                                    int32_t vgl_mask, double* out, void* cuda_stream);
 
+/* ---- Batched form: many molecules of uneven size evaluated together ----------------------
+ *
+ * A batch groups member contexts (each set up with the usual calls: nucleus, AO basis, MO
+ * basis, points) on one GPU. qmckl_batch_provide_mo_vgl_device computes the MO vgl of every
+ * member whose points changed since its last evaluation, with one persistent kernel per stage
+ * covering all members (point ordering, fused AO kernel, MO contraction), the stages captured
+ * once as a CUDA graph and replayed on later calls. Results land in the members' own caches:
+ * qmckl_get_mo_basis_mo_vgl_device(member, ...) then returns them without recomputation (and,
+ * in FP64 mode, qmckl_get_ao_basis_ao_vgl_device too). The batch's precision mode applies to
+ * the results of all its members. Errors are recorded in the first member's error slot.
+ * Destroy a batch before its members. No counterpart in the reference, whose API evaluates
+ * one context per call. */
+typedef int64_t qmckl_batch_device;
+#define QMCKL_NULL_BATCH_DEVICE ((qmckl_batch_device)0)
+/* members: member_num distinct valid contexts on the same device; QMCKL_NULL_BATCH_DEVICE on
+ * invalid arguments. */
+qmckl_batch_device qmckl_batch_create_device(const qmckl_context_device* members, int64_t member_num);
+qmckl_exit_code_device qmckl_batch_destroy_device(qmckl_batch_device batch);
+qmckl_exit_code_device qmckl_batch_set_precision_mode_device(qmckl_batch_device batch, int32_t mode);
+/* enable = 0 issues the stages as ordinary launches (per-kernel profiling of the first member
+ * applies then); 1 (default) replays a captured CUDA graph. */
+qmckl_exit_code_device qmckl_batch_set_graph_device(qmckl_batch_device batch, int32_t enable);
+/* async = 1: provide returns once the work is enqueued on the first member's stream; call
+ * qmckl_batch_synchronize_device before reading member results. */
+qmckl_exit_code_device qmckl_batch_set_async_device(qmckl_batch_device batch, int32_t async);
+qmckl_exit_code_device qmckl_batch_synchronize_device(qmckl_batch_device batch);
+qmckl_exit_code_device qmckl_batch_provide_mo_vgl_device(qmckl_batch_device batch);
+/* Touches every member (the next provide recomputes all of them). */
+qmckl_exit_code_device qmckl_batch_touch_device(qmckl_batch_device batch);
+/* Launch parameters, chosen by the built-in autotuner on the first provide of each batch shape
+ * (timed candidates; results cached per shape in the process and, when the environment
+ * variable QMCKL_GB300_TUNE_CACHE names a file, in that file):
+ *   params[0] nucleus-chunk level of the AO kernel's warp tasks (0 = whole molecule, v ~ 2^v chunks)
+ *   params[1] FP64 contraction CTA tile: 0 = 64x64, 1 = 128x64, 2 = 64x128
+ *   params[2] split-BF16 contraction: widest column tile (16..96, multiple of 16)
+ * set pins the parameters (n = 3; no autotuning afterwards); get reads them (-1 = not chosen yet);
+ * autotune re-times the candidates now (members must be ready to provide). */
+qmckl_exit_code_device qmckl_batch_set_tuning_device(qmckl_batch_device batch, const int32_t* params, int64_t n);
+qmckl_exit_code_device qmckl_batch_get_tuning_device(qmckl_batch_device batch, int32_t* params, int64_t n);
+qmckl_exit_code_device qmckl_batch_autotune_device(qmckl_batch_device batch);
+/* Kernels launched by one provide (all stages). */
+int64_t qmckl_batch_get_launch_count_device(qmckl_batch_device batch);
+
 /* Test hook for allocation failure handling: the n-th device allocation from now on
  * (n >= 1) fails as if cudaMalloc had failed; n = 0 disables the hook. */
 qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device context, int64_t n);

@@ -34,6 +34,7 @@ _SCALARS = {
     "void": None,
     "qmckl_exit_code_device": ctypes.c_int32,
     "qmckl_context_device": ctypes.c_int64,
+    "qmckl_batch_device": ctypes.c_int64,
     "int64_t": ctypes.c_int64,
     "int32_t": ctypes.c_int32,
     "uint64_t": ctypes.c_uint64,

@@ -56,6 +56,7 @@ class Context:
         if not self.handle:
             raise QmcklError(INVALID_CONTEXT, "qmckl_context_create_device", "context creation failed")
         self._buffers = {}
+        self.point_num = 0  # points of the last set_point
 
     # ------------------------------------------------------------------ lifetime
     def close(self):
@@ -164,6 +165,7 @@ class Context:
         num = c.shape[0] if transp == "N" else c.shape[1]
         ptr = c.ctypes.data_as(ctypes.c_void_p) if host else self.upload(c, key="points").ptr
         self.call("set_point", transp.encode(), num, ptr, 3 * num)
+        self.point_num = int(num)
 
     def load_system(self, s, mo=True, points=True):
         self.set_nucleus(s)
@@ -244,3 +246,76 @@ class Context:
 
     def launch_count(self):
         return self.L.qmckl_get_launch_count_device(self.handle)
+
+
+class Batch:
+    """Several member contexts evaluated together (qmckl_batch_*_device): one persistent launch
+    per stage over every member, replayed as a CUDA graph. Results land in the members' caches,
+    so `member.get_mo_vgl(P)` reads them afterwards."""
+
+    def __init__(self, members):
+        self.L = capi.lib()
+        self.members = list(members)
+        handles = (ctypes.c_int64 * len(self.members))(*[m.handle for m in self.members])
+        self.handle = self.L.qmckl_batch_create_device(handles, len(self.members))
+        if not self.handle:
+            raise QmcklError(INVALID_CONTEXT, "qmckl_batch_create_device", "batch creation failed")
+
+    def close(self):
+        if self.handle:
+            self.L.qmckl_batch_destroy_device(self.handle)
+            self.handle = 0
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def call(self, name, *args):
+        rc = getattr(self.L, "qmckl_batch_%s_device" % name)(self.handle, *args)
+        return self.members[0].check(rc, "qmckl_batch_%s_device" % name)
+
+    def set_precision(self, mode):
+        self.call("set_precision_mode", int(mode))
+
+    def set_graph(self, on):
+        self.call("set_graph", 1 if on else 0)
+
+    def set_async(self, on):
+        self.call("set_async", 1 if on else 0)
+
+    def synchronize(self):
+        self.call("synchronize")
+
+    def touch(self):
+        self.call("touch")
+
+    def provide_mo_vgl(self):
+        self.call("provide_mo_vgl")
+
+    def autotune(self):
+        self.call("autotune")
+
+    def tuning(self):
+        p = (ctypes.c_int32 * 3)()
+        self.call("get_tuning", p, 3)
+        return tuple(p)
+
+    def set_tuning(self, params):
+        p = (ctypes.c_int32 * 3)(*[int(x) for x in params])
+        self.call("set_tuning", p, 3)
+
+    def launch_count(self):
+        return self.L.qmckl_batch_get_launch_count_device(self.handle)
+
+    def get_mo_vgl(self):
+        """[member] -> numpy [P][5][M] (provides first)."""
+        self.provide_mo_vgl()
+        return [m.get_mo_vgl(m.point_num) for m in self.members]

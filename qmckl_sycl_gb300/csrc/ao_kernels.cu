@@ -289,41 +289,12 @@ __device__ __noinline__ void shell_generic(Writer<O>& w, double x, double y, dou
     }
 }
 
-struct FusedArgs {
-  const NucleusEntry* nuclei;
-  const ShellEntry* shells;
-  const PrimEntry* prims;
-  const double* aof;
-  const NucleusChunk* chunks;
-  const ExpTable* exp_table;
-  const double* coord;      // [3][P]
-  const int32_t* perm;      // processing order of the points, or null
-  double* out;              // Vgl / Value
-  __nv_bfloat16* planes;    // Planes
-  int64_t point_num;
-  int64_t ao_num;
-  int64_t row_len;          // ao_num, or kp for Planes
-  int64_t task_num;
-  int chunk_num;
-};
 
 // One warp task: 32 points (lane = point) x one chunk of consecutive nuclei.
 template <Out O>
-__global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a) {
+__device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
+                                        const double* __restrict__ thi, const double* __restrict__ tlo, int lane) {
   constexpr int NC = ncomp<O>();
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* thi = reinterpret_cast<double*>(smem_raw);
-  double* tlo = thi + 32;
-  if constexpr (NC == 5 || O == Out::Value) {
-    for (int i = threadIdx.x; i < 32; i += blockDim.x) {
-      thi[i] = a.exp_table->hi[i];
-      tlo[i] = a.exp_table->lo[i];
-    }
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
-  if (task >= a.task_num) return;  // warp-uniform
   const int64_t group = task / a.chunk_num;
   const int ch = (int)(task - group * a.chunk_num);
   const int64_t p0 = group * 32;
@@ -335,9 +306,9 @@ __global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a
   const double ex = a.coord[p], ey = a.coord[P + p], ez = a.coord[2 * P + p];
 
   Writer<O> w;
-  w.st = reinterpret_cast<Stage<NC>*>(smem_raw + 512) + warp;
+  w.st = st;
   w.out = a.out;
-  w.planes = a.planes;
+  w.planes = static_cast<__nv_bfloat16*>(a.planes);
   w.plane_stride = 5 * P * a.row_len;
   w.row_len = a.row_len;
   w.nvalid = nvalid;
@@ -414,6 +385,58 @@ __global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a
   w.flush();
 }
 
+// Loads the exponential's table into the first 512 bytes of dynamic shared memory.
+__device__ __forceinline__ void load_exp_table(const ExpTable* __restrict__ tab, double* thi, double* tlo) {
+  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+    thi[i] = tab->hi[i];
+    tlo[i] = tab->lo[i];
+  }
+}
+
+// One molecule: warp task = blockIdx.x * kWarps + warp.
+template <Out O>
+__global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* thi = reinterpret_cast<double*>(smem_raw);
+  double* tlo = thi + 32;
+  load_exp_table(a.exp_table, thi, tlo);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
+  if (task >= a.task_num) return;  // warp-uniform
+  ao_task<O>(a, task, reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + 512) + warp, thi, tlo, lane);
+}
+
+// Many molecules, persistent: each warp takes the next task from a global counter until the
+// tasks of every molecule are done (uneven molecules balance themselves).
+template <Out O>
+__global__ void __launch_bounds__(kWarps * 32) ao_batch_kernel(const FusedArgs* __restrict__ mols,
+                                                                const int64_t* __restrict__ task_begin, int nmol,
+                                                                int64_t total, unsigned long long* counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* thi = reinterpret_cast<double*>(smem_raw);
+  double* tlo = thi + 32;
+  load_exp_table(mols[0].exp_table, thi, tlo);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + 512) + warp;
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1ull);
+    t = __shfl_sync(kFull, t, 0);
+    if (t >= (unsigned long long)total) break;
+    const int64_t task = (int64_t)t;
+    int lo = 0, hi = nmol - 1;  // last molecule whose first task is <= task
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (task_begin[mid] <= task) lo = mid;
+      else hi = mid - 1;
+    }
+    const FusedArgs a = mols[lo];
+    ao_task<O>(a, task - task_begin[lo], st, thi, tlo, lane);
+  }
+}
+
 // Shell radials on their own (qmckl_get_ao_basis_shell_vgl_device), one thread per
 // (point, packed shell), the reference's formulas of src/qmckl_ao_sycl.cpp:47-95.
 __global__ void shell_vgl_kernel(const NucleusEntry* __restrict__ nuclei, const ShellEntry* __restrict__ shells,
@@ -455,25 +478,23 @@ __global__ void shell_vgl_kernel(const NucleusEntry* __restrict__ nuclei, const 
 }
 
 // ---------------------------------------------------------------- point order
+__device__ __forceinline__ int morton_key(double x, double y, double z, const double* origin, double inv_cell);
+
 // 15-bit Morton key of a point's cell on the 32^3 grid; one counter per cell.
 __global__ void morton_key_kernel(const double* __restrict__ coord, int64_t P, double ox, double oy, double oz,
                                   double inv_cell, int32_t* __restrict__ keys, int32_t* __restrict__ counts) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
-  const double c[3] = {(coord[p] - ox) * inv_cell, (coord[P + p] - oy) * inv_cell, (coord[2 * P + p] - oz) * inv_cell};
-  int key = 0;
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    int q = c[d] > 0.0 ? (c[d] < 31.0 ? (int)c[d] : 31) : 0;  // NaN goes to cell 0
-#pragma unroll
-    for (int b = 0; b < 5; ++b) key |= ((q >> b) & 1) << (3 * b + d);
-  }
+  const double origin[3] = {ox, oy, oz};
+  const int key = morton_key(coord[p], coord[P + p], coord[2 * P + p], origin, inv_cell);
   keys[p] = key;
   atomicAdd(&counts[key], 1);
 }
 
-// In-place exclusive prefix sum of the kOrderCells counters, one CTA of 1024 threads.
-__global__ void __launch_bounds__(1024) cell_scan_kernel(int32_t* __restrict__ counts) {
+// In-place exclusive prefix sum of kOrderCells counters per CTA of 1024 threads (CTA b scans
+// the counters of molecule b).
+__global__ void __launch_bounds__(1024) cell_scan_kernel(int32_t* __restrict__ counts_all) {
+  int32_t* __restrict__ counts = counts_all + (int64_t)blockIdx.x * kOrderCells;
   constexpr int kPer = kOrderCells / 1024;
   __shared__ int32_t part[1024];
   int32_t local[kPer];
@@ -520,11 +541,78 @@ int pick_level(const AoTables& t, int64_t groups, int sms) {
 }
 
 template <Out O>
+size_t fused_smem() {
+  return 512 + sizeof(Stage<ncomp<O>()>) * kWarps;
+}
+
+template <Out O>
 cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
                          double* out, __nv_bfloat16* planes, int64_t row_len, const char* name) {
   if (point_num <= 0 || t.ao_num <= 0) return cudaSuccess;
   const int64_t groups = (point_num + 31) / 32;
-  const int lv = pick_level(t, groups, t.sm_count);
+  const FusedArgs a = make_fused_args(t, pick_level(t, groups, t.sm_count), coord, perm, point_num, out, planes, row_len);
+  const int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
+  const size_t smem = fused_smem<O>();
+  cudaFuncSetAttribute(ao_fused_kernel<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  LaunchScope scope(ctx, name);
+  ao_fused_kernel<O><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a);
+  return cudaGetLastError();
+}
+
+__device__ __forceinline__ int morton_key(double x, double y, double z, const double* origin, double inv_cell) {
+  const double c[3] = {(x - origin[0]) * inv_cell, (y - origin[1]) * inv_cell, (z - origin[2]) * inv_cell};
+  int key = 0;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    int q = c[d] > 0.0 ? (c[d] < 31.0 ? (int)c[d] : 31) : 0;  // NaN goes to cell 0
+#pragma unroll
+    for (int b = 0; b < 5; ++b) key |= ((q >> b) & 1) << (3 * b + d);
+  }
+  return key;
+}
+
+// Molecule owning global point gp: the last m with point_begin[m] <= gp.
+__device__ __forceinline__ int owner_of(const int64_t* __restrict__ point_begin, int nmol, int64_t gp) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (point_begin[mid] <= gp) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void batch_key_kernel(const OrderDesc* __restrict__ desc, const int64_t* __restrict__ point_begin, int nmol,
+                                 int64_t total, int32_t* __restrict__ counts) {
+  const int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gp >= total) return;
+  const int m = owner_of(point_begin, nmol, gp);
+  const OrderDesc& d = desc[m];
+  const int64_t p = gp - point_begin[m];
+  const int64_t P = d.point_num;
+  const int key = morton_key(d.coord[p], d.coord[P + p], d.coord[2 * P + p], d.origin, d.inv_cell);
+  d.keys[p] = key;
+  atomicAdd(&counts[(int64_t)m * kOrderCells + key], 1);
+}
+
+__global__ void batch_scatter_kernel(const OrderDesc* __restrict__ desc, const int64_t* __restrict__ point_begin,
+                                     int nmol, int64_t total, int32_t* __restrict__ offsets) {
+  const int64_t gp = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gp >= total) return;
+  const int m = owner_of(point_begin, nmol, gp);
+  const OrderDesc& d = desc[m];
+  const int64_t p = gp - point_begin[m];
+  const int pos = atomicAdd(&offsets[(int64_t)m * kOrderCells + d.keys[p]], 1);
+  d.perm[pos] = (int32_t)p;
+}
+
+}  // namespace
+
+int ao_level_count(const AoTables& t) { return (int)t.level_offsets.size(); }
+
+FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
+                          double* out, void* planes, int64_t row_len) {
+  const int lv = level < 0 ? 0 : (level >= (int)t.level_offsets.size() ? (int)t.level_offsets.size() - 1 : level);
   FusedArgs a;
   a.nuclei = t.nuclei;
   a.shells = t.shells;
@@ -540,16 +628,55 @@ cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, const
   a.point_num = point_num;
   a.ao_num = t.ao_num;
   a.row_len = row_len;
-  a.task_num = groups * a.chunk_num;
-  const int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
-  const size_t smem = 512 + sizeof(Stage<ncomp<O>()>) * kWarps;
-  cudaFuncSetAttribute(ao_fused_kernel<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  LaunchScope scope(ctx, name);
-  ao_fused_kernel<O><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a);
+  a.task_num = ((point_num + 31) / 32) * a.chunk_num;
+  return a;
+}
+
+int ao_batch_resident_ctas(bool planes) {
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (planes) {
+    cudaFuncSetAttribute(ao_batch_kernel<Out::Planes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)fused_smem<Out::Planes>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ao_batch_kernel<Out::Planes>, kWarps * 32,
+                                                  fused_smem<Out::Planes>());
+  } else {
+    cudaFuncSetAttribute(ao_batch_kernel<Out::Vgl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)fused_smem<Out::Vgl>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ao_batch_kernel<Out::Vgl>, kWarps * 32,
+                                                  fused_smem<Out::Vgl>());
+  }
+  cudaGetLastError();
+  return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, const FusedArgs* mols, const int64_t* task_begin,
+                            int nmol, int64_t total, unsigned long long* counter, int grid) {
+  if (nmol <= 0 || total <= 0) return cudaSuccess;
+  if (grid <= 0) grid = ao_batch_resident_ctas(planes);
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  if (planes)
+    ao_batch_kernel<Out::Planes><<<grid, kWarps * 32, fused_smem<Out::Planes>(), stream>>>(mols, task_begin, nmol,
+                                                                                          total, counter);
+  else
+    ao_batch_kernel<Out::Vgl><<<grid, kWarps * 32, fused_smem<Out::Vgl>(), stream>>>(mols, task_begin, nmol, total,
+                                                                                    counter);
   return cudaGetLastError();
 }
 
-}  // namespace
+cudaError_t launch_order_batch(cudaStream_t stream, const OrderDesc* desc, const int64_t* point_begin, int nmol,
+                               int64_t total_points, int32_t* counts) {
+  if (nmol <= 0 || total_points <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * kOrderCells * (size_t)nmol, stream);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((total_points + 255) / 256);
+  batch_key_kernel<<<blocks, 256, 0, stream>>>(desc, point_begin, nmol, total_points, counts);
+  cell_scan_kernel<<<nmol, 1024, 0, stream>>>(counts);
+  batch_scatter_kernel<<<blocks, 256, 0, stream>>>(desc, point_begin, nmol, total_points, counts);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int32_t* keys,
                                int32_t* counts, int32_t* perm) {

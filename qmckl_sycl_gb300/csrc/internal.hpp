@@ -298,6 +298,78 @@ cudaError_t launch_mo_vgl_fp64(Ctx* ctx, const double* ao_vgl, const double* coe
 cudaError_t launch_mo_value_fp64(Ctx* ctx, const double* ao_value, const double* coef_t, int64_t point_num,
                                  int64_t ao_num, int64_t mo_num, double* mo_value);
 cudaError_t launch_transpose(Ctx* ctx, const double* in, int64_t rows, int64_t cols, double* out);
+
+// ---- multi-molecule (batched) launches: one launch covers the work of every molecule ----
+// Arguments of the fused AO kernel for one molecule (one warp task = 32 points x one
+// nucleus chunk of the selected level).
+struct FusedArgs {
+  const NucleusEntry* nuclei;
+  const ShellEntry* shells;
+  const PrimEntry* prims;
+  const double* aof;
+  const NucleusChunk* chunks;
+  const ExpTable* exp_table;
+  const double* coord;      // [3][P]
+  const int32_t* perm;      // processing order of the points, or null
+  double* out;              // ao_vgl (FP64 output)
+  void* planes;             // BF16 planes [3][5P][row_len] (split-BF16 output)
+  int64_t point_num;
+  int64_t ao_num;
+  int64_t row_len;          // ao_num, or the padded K of the planes
+  int64_t task_num;
+  int chunk_num;
+};
+// Number of nucleus-chunk levels of the tables (level v has about 2^v chunks).
+int ao_level_count(const AoTables& t);
+FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
+                          double* out, void* planes, int64_t row_len);
+// Persistent AO kernel over the tasks of nmol molecules: mols[m]'s tasks are numbered from
+// task_begin[m] (non-decreasing, task_begin[nmol] = total); warps take tasks from *counter
+// (zeroed before the launch). planes selects the BF16-plane output. grid <= 0: resident CTAs.
+cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, const FusedArgs* mols, const int64_t* task_begin,
+                            int nmol, int64_t total, unsigned long long* counter, int grid);
+int ao_batch_resident_ctas(bool planes);
+
+// Point order of nmol molecules at once: one Morton grid per molecule, counts [nmol][kOrderCells].
+struct OrderDesc {
+  const double* coord;  // [3][P]
+  int64_t point_num;
+  int64_t point_begin;  // first global point index of the molecule
+  double origin[3];
+  double inv_cell;
+  int32_t* keys;        // [P]
+  int32_t* perm;        // [P]
+};
+cudaError_t launch_order_batch(cudaStream_t stream, const OrderDesc* desc, const int64_t* point_begin, int nmol,
+                               int64_t total_points, int32_t* counts);
+
+// FP64 contraction of several molecules in one persistent launch; CTA tiles are taken from
+// *counter (zeroed before the launch) in job order. shape: 0 = 64x64, 1 = 128x64, 2 = 64x128.
+struct GemmJob {
+  const double* a;  // [rows][k]
+  const double* b;  // [k][cols]
+  double* c;        // [rows][cols]
+  int64_t rows, k, cols;
+  int32_t col_tiles;
+  int32_t tile_begin;
+};
+constexpr int kGemmShapes = 3;
+void gemm_shape_tile(int shape, int* rows, int* cols);
+cudaError_t launch_dgemm_batch(cudaStream_t stream, int shape, bool mask5, const GemmJob* jobs, const int32_t* tile_begin,
+                               int njobs, int total_tiles, unsigned int* counter);
+
+// Split-BF16 contraction of several molecules: host-built descriptors (opaque here).
+size_t split_job_bytes();
+// Writes one job (out[rows][M] from A planes [3][rows][kp] and B planes [3][M][kp]) into
+// job_host with column tiles of at most n_cap (16..96) columns; returns its tile count or -1.
+int split_make_job(void* job_host, const void* a_planes, int64_t rows, const void* b_planes, int64_t M, int64_t kp,
+                   double* out, int tile_begin, int n_cap);
+cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, int total_tiles, int* err);
+int64_t split_k_pad(int64_t ao_num);
+// The member's coefficient planes for the split-BF16 form (built once per coefficient set)
+// and its AO-plane buffer for rows x kp (returns null on allocation failure).
+qmckl_exit_code_device split_prepare_coef(Ctx* ctx, qmckl_context_device c, int64_t kp);
+void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp);
 cudaError_t launch_strided_copy(Ctx* ctx, const double* in, int64_t in_stride, double* out, int64_t out_stride,
                                 int64_t rows, int64_t cols);
 cudaError_t launch_fill(Ctx* ctx, double* p, int64_t n, double v);

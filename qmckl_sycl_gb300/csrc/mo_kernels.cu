@@ -46,14 +46,13 @@ __device__ __forceinline__ double load_a(const double* __restrict__ A, int64_t R
   return v;
 }
 
+// One warp's 32x32 tile of C at (r0, c0), if it starts inside C.
 template <bool MASK>
-__global__ void __launch_bounds__(128) dgemm_dmma_kernel(const double* __restrict__ A, const double* __restrict__ B,
-                                                         double* __restrict__ C, int64_t R, int64_t K, int64_t N) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int g = lane >> 2, t = lane & 3;
-  const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
-  const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
+__device__ __forceinline__ void dgemm_warp_tile(const double* __restrict__ A, const double* __restrict__ B,
+                                                double* __restrict__ C, int64_t R, int64_t K, int64_t N, int64_t r0,
+                                                int64_t c0, int lane) {
   if (r0 >= R || c0 >= N) return;  // warp-uniform
+  const int g = lane >> 2, t = lane & 3;
   double acc[2][4][4];
 #pragma unroll
   for (int i = 0; i < 2; ++i)
@@ -99,6 +98,58 @@ __global__ void __launch_bounds__(128) dgemm_dmma_kernel(const double* __restric
 }
 
 template <bool MASK>
+__global__ void __launch_bounds__(128) dgemm_dmma_kernel(const double* __restrict__ A, const double* __restrict__ B,
+                                                         double* __restrict__ C, int64_t R, int64_t K, int64_t N) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
+  const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
+  dgemm_warp_tile<MASK>(A, B, C, R, K, N, r0, c0, lane);
+}
+
+// Several contractions, persistent: a CTA of WR x WC warps owns (32 WR) x (32 WC) tiles of C,
+// taken from *counter in job order (the host lists the jobs with the longest K first).
+template <bool MASK, int WR, int WC>
+__global__ void __launch_bounds__(32 * WR * WC) dgemm_batch_kernel(const GemmJob* __restrict__ jobs,
+                                                                    const int32_t* __restrict__ tile_begin, int njobs,
+                                                                    int total_tiles, unsigned int* counter) {
+  __shared__ int s_tile;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    __syncthreads();
+    if (tile >= total_tiles) break;
+    int lo = 0, hi = njobs - 1;  // last job whose first tile is <= tile
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tile_begin[mid] <= tile) lo = mid;
+      else hi = mid - 1;
+    }
+    const GemmJob& jb = jobs[lo];
+    const int local = tile - tile_begin[lo];
+    const int64_t r0 = (int64_t)(local / jb.col_tiles) * (32 * WR) + (warp / WC) * 32;
+    const int64_t c0 = (int64_t)(local % jb.col_tiles) * (32 * WC) + (warp % WC) * 32;
+    dgemm_warp_tile<MASK>(jb.a, jb.b, jb.c, jb.rows, jb.k, jb.cols, r0, c0, lane);
+  }
+}
+
+template <bool MASK, int WR, int WC>
+cudaError_t launch_batch_shape(cudaStream_t stream, const GemmJob* jobs, const int32_t* tile_begin, int njobs,
+                               int total_tiles, unsigned int* counter) {
+  int dev = 0, sms = 152, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dgemm_batch_kernel<MASK, WR, WC>, 32 * WR * WC, 0);
+  int grid = sms * (per_sm > 0 ? per_sm : 1);
+  if (grid > total_tiles) grid = total_tiles;
+  cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream);
+  if (e != cudaSuccess) return e;
+  dgemm_batch_kernel<MASK, WR, WC><<<grid, 32 * WR * WC, 0, stream>>>(jobs, tile_begin, njobs, total_tiles, counter);
+  return cudaGetLastError();
+}
+
+template <bool MASK>
 cudaError_t launch_dgemm(Ctx* ctx, const double* A, const double* B, double* C, int64_t R, int64_t K, int64_t N,
                          const char* name) {
   if (R <= 0 || N <= 0) return cudaSuccess;
@@ -110,6 +161,25 @@ cudaError_t launch_dgemm(Ctx* ctx, const double* A, const double* B, double* C, 
 }
 
 }  // namespace
+
+void gemm_shape_tile(int shape, int* rows, int* cols) {
+  *rows = shape == 1 ? 128 : 64;
+  *cols = shape == 2 ? 128 : 64;
+}
+
+cudaError_t launch_dgemm_batch(cudaStream_t stream, int shape, bool mask5, const GemmJob* jobs,
+                               const int32_t* tile_begin, int njobs, int total_tiles, unsigned int* counter) {
+  if (njobs <= 0 || total_tiles <= 0) return cudaSuccess;
+  switch (shape * 2 + (mask5 ? 1 : 0)) {
+    case 0: return launch_batch_shape<false, 2, 2>(stream, jobs, tile_begin, njobs, total_tiles, counter);
+    case 1: return launch_batch_shape<true, 2, 2>(stream, jobs, tile_begin, njobs, total_tiles, counter);
+    case 2: return launch_batch_shape<false, 4, 2>(stream, jobs, tile_begin, njobs, total_tiles, counter);
+    case 3: return launch_batch_shape<true, 4, 2>(stream, jobs, tile_begin, njobs, total_tiles, counter);
+    case 4: return launch_batch_shape<false, 2, 4>(stream, jobs, tile_begin, njobs, total_tiles, counter);
+    case 5: return launch_batch_shape<true, 2, 4>(stream, jobs, tile_begin, njobs, total_tiles, counter);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t launch_mo_vgl_fp64(Ctx* ctx, const double* ao_vgl, const double* coef_t, int64_t point_num,
                                int64_t ao_num, int64_t mo_num, double* mo_vgl) {

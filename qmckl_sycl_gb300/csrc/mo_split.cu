@@ -270,8 +270,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   int done_phases = 0;  // mma_done completions so far (one per tile with MMAs issued)
   for (int tile = blockIdx.x; tile < total_tiles && !*abort_flag; tile += gridDim.x) {
-    int j = 0;
-    while (j + 1 < njobs && jobs[j + 1].tile_begin <= tile) ++j;
+    int j = 0, hi = njobs - 1;  // last job whose first tile is <= tile
+    while (j < hi) {
+      const int mid = (j + hi + 1) >> 1;
+      if (jobs[mid].tile_begin <= tile) j = mid;
+      else hi = mid - 1;
+    }
     const SplitJob& job = jobs[j];
     const int local = tile - job.tile_begin;
     const int N = job.n_tile;
@@ -473,17 +477,18 @@ int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 // Column tiling of an M-column contraction: the fewest tiles of at most kMaxN columns,
 // as equal as multiples of 16 allow.
-int tile_cols(int64_t M) {
-  const int ntiles = (int)((M + kMaxN - 1) / kMaxN);
+int tile_cols(int64_t M, int cap = kMaxN) {
+  cap = cap < 16 ? 16 : (cap > kMaxN ? kMaxN : cap / 16 * 16);
+  const int ntiles = (int)((M + cap - 1) / cap);
   return (int)round_up((M + ntiles - 1) / ntiles, 16);
 }
 
 // Describes out[rows][M] = A planes (ap, [3][rows][kp]) x B planes (bp, [3][M][kp])^T as a
 // job whose tiles start at tile_begin; returns its tile count, or -1 if a map fails.
 int make_job(SplitJob& job, const __nv_bfloat16* ap, int64_t rows, const __nv_bfloat16* bp, int64_t M, int64_t kp,
-             double* out, int tile_begin) {
+             double* out, int tile_begin, int n_cap = kMaxN) {
   memset(&job, 0, sizeof job);
-  const int n_tile = tile_cols(M);
+  const int n_tile = tile_cols(M, n_cap);
   for (int i = 0; i < 3; ++i)
     if (!encode_map(&job.ta[i], ap + (size_t)i * rows * kp, rows, kp, kBM) ||
         !encode_map(&job.tb[i], bp + (size_t)i * M * kp, M, kp, n_tile))
@@ -616,6 +621,28 @@ static qmckl_exit_code_device split_mo_vgl(Ctx* ctx, qmckl_context_device c, dou
   __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(ctx->mo_basis.ao_split);
   launch_ao_planes(ctx, ctx->ao_basis.tables, ctx->point.coord, point_order(ctx), P, kp, ap);
   return contract_planes(ctx, c, ap, rows, kp, err, out, "mo_vgl_split_bf16");
+}
+
+size_t split_job_bytes() { return sizeof(SplitJob); }
+
+int split_make_job(void* job_host, const void* a_planes, int64_t rows, const void* b_planes, int64_t M, int64_t kp,
+                   double* out, int tile_begin, int n_cap) {
+  return make_job(*static_cast<SplitJob*>(job_host), static_cast<const __nv_bfloat16*>(a_planes), rows,
+                  static_cast<const __nv_bfloat16*>(b_planes), M, kp, out, tile_begin, n_cap);
+}
+
+cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, int total_tiles, int* err) {
+  return launch_split_jobs(stream, static_cast<const SplitJob*>(jobs), njobs, total_tiles, err);
+}
+
+int64_t split_k_pad(int64_t ao_num) { return round_up(ao_num, kBK); }
+
+qmckl_exit_code_device split_prepare_coef(Ctx* ctx, qmckl_context_device c, int64_t kp) {
+  return ensure_coef_planes(ctx, c, kp);
+}
+
+void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
+  return ensure_a_planes(ctx, rows, kp) ? ctx->mo_basis.ao_split : nullptr;
 }
 
 qmckl_exit_code_device provide_mo_split(Ctx* ctx, qmckl_context_device c, double* dst, bool value_only) {

@@ -52,6 +52,21 @@ def test_null_context_codes():
     assert L.qmckl_string_of_error_device(103) == b"Invalid context"
 
 
+def test_batch_argument_checks():
+    # creation rejects empty, invalid and duplicated member lists before touching a GPU
+    assert L.qmckl_batch_create_device(None, 0) == 0
+    bad = (ctypes.c_int64 * 2)(0, 0)
+    assert L.qmckl_batch_create_device(bad, 2) == 0
+    c = L.qmckl_context_create_device(0)
+    dup = (ctypes.c_int64 * 2)(c, c)
+    assert L.qmckl_batch_create_device(dup, 2) == 0
+    assert L.qmckl_context_destroy_device(c) == 0
+    for f in ("destroy", "touch", "provide_mo_vgl", "synchronize", "autotune"):
+        assert getattr(L, "qmckl_batch_%s_device" % f)(0) == 103
+    assert L.qmckl_batch_set_precision_mode_device(0, 1) == 103
+    assert L.qmckl_batch_get_launch_count_device(0) == 0
+
+
 def test_error_record_and_strings():
     c = L.qmckl_context_create_device(0)
     assert L.qmckl_context_check_device(c) == c
