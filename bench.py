@@ -46,6 +46,7 @@ def parse():
     p.add_argument("--electrons", type=int, default=160)
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the 64-molecule batched-form measurement")
     return p.parse_args()
 
 
@@ -286,6 +287,93 @@ def time_e2e(ctx, s, steps, warmup):
     return dt, coord.nbytes, out.nbytes, out
 
 
+def time_batched(dist, steps, warmup, peaks, fp64_peak):
+    """The batched form on the 64-molecule workload: every member's MO vgl per step through
+    qmckl_batch_provide_mo_vgl_device (graph replay, autotuned), both precision forms, plus
+    one profiled pass with ordinary launches for the per-stage times."""
+    from qmckl_sycl_gb300 import Batch, Context, config_batched
+
+    systems = config_batched(0)
+    ctxs = []
+    for sy in systems:
+        c = Context(dist.local_rank)
+        c.load_system(sy)
+        ctxs.append(c)
+    lead = ctxs[0]
+    b = Batch(ctxs)
+    P = sum(sy.point_num for sy in systems)
+    ao_bytes = {"fp64": sum((8.0 * 5 * sy.ao_num + 24.0) * sy.point_num for sy in systems),
+                "mixed": sum((6.0 * 5 * sy.ao_num + 24.0) * sy.point_num for sy in systems)}
+    flops = sum(10.0 * sy.ao_num * sy.mo_num * sy.point_num for sy in systems)
+    out = {"workload": "batched: %d molecules (%d-%d nuclei, %d-%d AOs, %d-%d MOs), 32 walkers x 2N electrons "
+                       "each, %d points in total" % (
+                           len(systems), min(x.nucl_num for x in systems), max(x.nucl_num for x in systems),
+                           min(x.ao_num for x in systems), max(x.ao_num for x in systems),
+                           min(x.mo_num for x in systems), max(x.mo_num for x in systems), P),
+           "point_num": P, "forms": {}}
+    ref = None
+    for form, mode in (("fp64", 0), ("mixed", 1)):
+        b.set_precision(mode)
+        b.set_async(False)
+        b.touch()
+        b.provide_mo_vgl()  # autotunes this shape, captures the graph
+        b.set_async(True)
+        for _ in range(warmup):
+            b.touch()
+            b.provide_mo_vgl()
+        b.synchronize()
+        dist.barrier()
+        lead.call("timer_start")
+        for _ in range(steps):
+            b.touch()
+            b.provide_mo_vgl()
+        ms = ctypes.c_double(0)
+        lead.call("timer_stop", ctypes.byref(ms))
+        b.synchronize()
+        b.set_async(False)
+        t = dist.max(ms.value)
+        lead.set_profiling(True)
+        lead.reset_kernel_stats()
+        for _ in range(2):
+            b.touch()
+            b.provide_mo_vgl()
+        stats = lead.kernel_stats()
+        lead.set_profiling(False)
+        kern = {}
+        for k, st in stats.items():
+            n, tot = st
+            if n <= 0:
+                continue
+            kms = tot / n
+            if k.startswith("batch_ao_vgl"):
+                a = ao_bytes[form] / (kms * 1e-3) / 1e9
+                kern[k] = {"bound": "hbm", "achieved": a, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                           "ms_per_launch": kms, "frac": a / peaks["hbm_gbs"]}
+            elif k.startswith("batch_mo_vgl"):
+                pk = fp64_peak if form == "fp64" else peaks.get("bf16_tflops", 1909.5)
+                a = flops / (kms * 1e-3) / 1e12
+                kern[k] = {"bound": "tensor", "achieved": a, "peak": pk, "unit": "TFLOP/s", "ms_per_launch": kms,
+                           "frac": a / pk}
+            else:
+                kern[k] = {"ms_per_launch": kms}
+        out["forms"][form] = {"value": dist.sum(P * steps) / (t * 1e-3), "ms_per_step": t / steps,
+                              "tuning": list(b.tuning()), "launches_per_step": b.launch_count(),
+                              "graph": True, "kernels": kern}
+        if form == "fp64":
+            ref = [c.get_mo_vgl(sy.point_num) for c, sy in zip(ctxs, systems)]
+        else:
+            worst = np.zeros(5)
+            for c, sy, r in zip(ctxs, systems, ref):
+                g = c.get_mo_vgl(sy.point_num)
+                worst = np.maximum(worst, np.abs(g - r).max(axis=(0, 2)) / np.abs(r).max(axis=(0, 2)))
+            out["mixed_vs_fp64_error"] = {"max_rel_normwise_over_molecules": [float(x) for x in worst]}
+    out["mixed_over_fp64"] = out["forms"]["mixed"]["value"] / out["forms"]["fp64"]["value"]
+    b.close()
+    for c in ctxs:
+        c.close()
+    return out
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -380,6 +468,10 @@ def main():
         v, cores, sample = cpu_baseline(s, args.cpu_seconds)
         cpu = {"value": v, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample}
 
+    bt = None
+    if not args.no_batched:
+        bt = time_batched(dist, args.steps, args.warmup, peaks, fp64_peak.value)
+        bt["mixed_over_plain_fp64_medium"] = bt["forms"]["mixed"]["value"] / results["fp64"]["value"]
     if dist.rank != 0:
         return
     hr = results[headline]
@@ -399,6 +491,8 @@ def main():
     if acc:
         line["mixed_vs_fp64_error"] = acc
         line["mixed_over_fp64"] = results["mixed"]["value"] / results["fp64"]["value"]
+    if bt:
+        line["batched"] = bt
     print(json.dumps(line), flush=True)
     ctx.close()
 
