@@ -65,6 +65,9 @@ def lib():
         L.oracle_shell_vgl.argtypes = [_I, _I, _I, _i64, _i64, _f64, _i64, _i64, _f64, _f64, _f64, _f64, _f64]
         L.oracle_mo_vgl.argtypes = [_I, _I, _I, _f64, _f64, _f64]
         L.oracle_mo_value.argtypes = [_I, _I, _I, _f64, _f64, _f64]
+        L.oracle_vjp_mo_vgl.restype = ctypes.c_int
+        L.oracle_vjp_mo_vgl.argtypes = [_I, _f64, _I, _I, _I, _i64, _i64, _i32, _i64, _i64, _f64, _f64, _f64, _f64,
+                                        _f64, _I, _f64, _I, _f64, _f64, _vp, _vp, _vp]
         _lib = L
     return _lib
 
@@ -117,6 +120,29 @@ def forward(s, coord_soa=None, want=("ao_vgl", "ao_value", "mo_vgl", "mo_value")
     rc = L.oracle_forward(*_basis_args(s), s.mo_num, s.mo_coef, P, np.ascontiguousarray(coord_soa),
                           _ptr(out.get("ao_vgl")), _ptr(out.get("ao_value")), _ptr(out.get("mo_vgl")),
                           _ptr(out.get("mo_value")))
+    assert rc == 0
+    return out
+
+
+def vjp_mo_vgl(s, w, want=("coef", "expo", "coord"), coord_soa=None, threads=0):
+    """FP64 reference gradient of L = sum(w * mo_vgl) for System s: dL/dC [M][A], dL/dexponent
+    [K] and dL/dcoord [P][3]. w is [P][5][M]."""
+    L = lib()
+    if threads:
+        L.oracle_set_num_threads(int(threads))
+    if coord_soa is None:
+        coord_soa = np.ascontiguousarray(s.coord.T)
+    P = coord_soa.shape[1]
+    out = {}
+    if "coef" in want:
+        out["coef"] = np.zeros((s.mo_num, s.ao_num))
+    if "expo" in want:
+        out["expo"] = np.zeros(s.prim_num)
+    if "coord" in want:
+        out["coord"] = np.zeros((P, 3))
+    rc = L.oracle_vjp_mo_vgl(*_basis_args(s), s.mo_num, s.mo_coef, P, np.ascontiguousarray(coord_soa),
+                             np.ascontiguousarray(w, dtype=np.float64), _ptr(out.get("coef")), _ptr(out.get("expo")),
+                             _ptr(out.get("coord")))
     assert rc == 0
     return out
 

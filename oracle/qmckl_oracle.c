@@ -446,3 +446,201 @@ int oracle_forward(int64_t nucl_num, const double* nucl_coord, int64_t shell_num
   free(nrange);
   return 0;
 }
+
+/* ======================================================================================
+ * FP64 reference gradient of L = sum_{p,l,m} w[p][l][m] * mo_vgl[p][l][m] (the adjoint form).
+ * The reference library has no derivatives; this is the oracle's own restatement, written
+ * per primitive (each primitive's contribution c e^{-a r^2} P(x,y,z) differentiated on its
+ * own), so that it shares no aggregation with the GPU kernels. Forward quantities come from
+ * the functions above (the reference's arithmetic); the MO kernel's zero-value skip
+ * (src/qmckl_mo_sycl.cpp:40) is a constant mask: where ao_vgl[p][0][k] == 0 no component of
+ * AO k contributes, so no gradient flows through it. Screening decisions are held fixed.
+ *
+ *   d_coef [mo_num][ao_num]  dL/dC for the user's coefficient layout
+ *   d_expo [prim_num]        dL/dexponent (user primitive order)
+ *   d_coord [point_num][3]   dL/d(point coordinates)
+ * ====================================================================================== */
+
+/* d^(dx+dy+dz) (x^a y^b z^c) / dx^dx dy^dy dz^dz */
+static double mono_deriv(int a, int b, int c, int dx, int dy, int dz, double x, double y, double z) {
+  if (dx > a || dy > b || dz > c) return 0.0;
+  double f = 1.0;
+  for (int i = 0; i < dx; ++i) f *= (double)(a - i);
+  for (int i = 0; i < dy; ++i) f *= (double)(b - i);
+  for (int i = 0; i < dz; ++i) f *= (double)(c - i);
+  for (int i = 0; i < a - dx; ++i) f *= x;
+  for (int i = 0; i < b - dy; ++i) f *= y;
+  for (int i = 0; i < c - dz; ++i) f *= z;
+  return f;
+}
+
+/* derivative multi-index of axis j added to (d0,d1,d2) */
+#define OR_D(P, d0, d1, d2) mono_deriv(a, b, c, (d0), (d1), (d2), x, y, z)
+
+int oracle_vjp_mo_vgl(int64_t nucl_num, const double* nucl_coord, int64_t shell_num, int64_t prim_num, int64_t ao_num,
+                      const int64_t* nucleus_index, const int64_t* nucleus_shell_num, const int32_t* shell_ang_mom,
+                      const int64_t* shell_prim_num, const int64_t* shell_prim_index, const double* shell_factor,
+                      const double* exponent, const double* coefficient, const double* prim_factor,
+                      const double* ao_factor, int64_t mo_num, const double* mo_coef, int64_t point_num,
+                      const double* coord, const double* w, double* d_coef, double* d_expo, double* d_coord) {
+  int64_t* nucleus_prim_index = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nucl_num + 1));
+  double* coef_norm = (double*)malloc(sizeof(double) * (size_t)prim_num);
+  int32_t* nmax = (int32_t*)malloc(sizeof(int32_t) * (size_t)nucl_num);
+  double* nrange = (double*)malloc(sizeof(double) * (size_t)nucl_num);
+  oracle_finalize_ao(nucl_num, shell_num, prim_num, nucleus_index, nucleus_shell_num, shell_ang_mom,
+                     shell_prim_index, shell_prim_num, exponent, coefficient, prim_factor, shell_factor,
+                     nucleus_prim_index, coef_norm, nmax, nrange);
+  double* shell_vgl = (double*)calloc((size_t)(point_num * 5 * shell_num), sizeof(double));
+  oracle_shell_vgl(point_num, nucl_num, shell_num, nucleus_index, nucleus_shell_num, nrange, shell_prim_index,
+                   shell_prim_num, coord, nucl_coord, exponent, coef_norm, shell_vgl);
+  double* ao = (double*)calloc((size_t)(point_num * 5 * ao_num), sizeof(double));
+  oracle_ao_vgl(point_num, nucl_num, shell_num, ao_num, nucleus_index, nucleus_shell_num, coord, nucl_coord, nrange,
+                nmax, shell_ang_mom, ao_factor, shell_vgl, ao);
+  int32_t* s2n = (int32_t*)malloc(sizeof(int32_t) * (size_t)shell_num);
+  int64_t* ao_index = (int64_t*)malloc(sizeof(int64_t) * (size_t)shell_num);
+  shell_to_nucleus(nucl_num, nucleus_index, nucleus_shell_num, shell_num, s2n);
+  shell_ao_index(nucl_num, nucleus_index, nucleus_shell_num, shell_ang_mom, ao_index);
+  const int nthreads = oracle_num_threads();
+  double* dc_all = d_coef ? (double*)calloc((size_t)nthreads * (size_t)(mo_num * ao_num), sizeof(double)) : NULL;
+  double* de_all = d_expo ? (double*)calloc((size_t)nthreads * (size_t)prim_num, sizeof(double)) : NULL;
+
+#pragma omp parallel
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double* gbar = (double*)malloc(sizeof(double) * (size_t)(5 * ao_num));
+    double* dc = dc_all ? dc_all + (size_t)tid * (size_t)(mo_num * ao_num) : NULL;
+    double* de = de_all ? de_all + (size_t)tid * (size_t)prim_num : NULL;
+#pragma omp for schedule(dynamic, 4)
+    for (int64_t p = 0; p < point_num; ++p) {
+      const double* a_p = ao + p * 5 * ao_num;
+      const double* w_p = w + p * 5 * mo_num;
+      /* adjoint of the AO values: gbar[l][k] = sum_m w[l][m] C[m][k], masked */
+      for (int64_t l = 0; l < 5; ++l)
+        for (int64_t k = 0; k < ao_num; ++k) {
+          double s = 0.0;
+          if (a_p[k] != 0.0)
+            for (int64_t m = 0; m < mo_num; ++m) s += w_p[l * mo_num + m] * mo_coef[m * ao_num + k];
+          gbar[l * ao_num + k] = s;
+        }
+      if (dc)
+        for (int64_t k = 0; k < ao_num; ++k) {
+          if (a_p[k] == 0.0) continue;
+          for (int64_t l = 0; l < 5; ++l) {
+            const double av = a_p[l * ao_num + k];
+            for (int64_t m = 0; m < mo_num; ++m) dc[m * ao_num + k] += w_p[l * mo_num + m] * av;
+          }
+        }
+      if (!de && !d_coord) continue;
+      double gc[3] = {0.0, 0.0, 0.0};
+      for (int64_t is = 0; is < shell_num; ++is) {
+        const int64_t n = s2n[is];
+        const double x = coord[p] - nucl_coord[n];
+        const double y = coord[p + point_num] - nucl_coord[n + nucl_num];
+        const double z = coord[p + 2 * point_num] - nucl_coord[n + 2 * nucl_num];
+        const double r2 = x * x + y * y + z * z;
+        if (r2 > ORACLE_CUTOFF * nrange[n]) continue;
+        const double xv[3] = {x, y, z};
+        const int L = shell_ang_mom[is];
+        for (int64_t q = shell_prim_index[is]; q < shell_prim_index[is] + shell_prim_num[is]; ++q) {
+          const double al = exponent[q];
+          const double ar2 = al * r2;
+          if (ar2 > ORACLE_CUTOFF) continue;
+          const double v = coef_norm[q] * exp(-ar2);
+          /* v and its derivatives: dv_j = -2 a x_j v; d2v_jd = (4 a^2 x_j x_d - 2 a delta_jd) v;
+             lap v = (4 a^2 r2 - 6 a) v; d_j lap v = (8 a^2 x_j + (4 a^2 r2 - 6 a)(-2 a x_j)) v */
+          double dv[3], d2v[3][3], dlapv[3];
+          const double lapv = (4.0 * al * al * r2 - 6.0 * al) * v;
+          for (int j = 0; j < 3; ++j) {
+            dv[j] = -2.0 * al * xv[j] * v;
+            for (int d = 0; d < 3; ++d) d2v[j][d] = (4.0 * al * al * xv[j] * xv[d] - (j == d ? 2.0 * al : 0.0)) * v;
+            dlapv[j] = 8.0 * al * al * xv[j] * v + (4.0 * al * al * r2 - 6.0 * al) * dv[j];
+          }
+          /* derivatives with respect to the exponent */
+          const double v_a = -r2 * v;
+          double dv_a[3];
+          for (int j = 0; j < 3; ++j) dv_a[j] = -2.0 * xv[j] * v - 2.0 * al * xv[j] * v_a;
+          const double lapv_a = (8.0 * al * r2 - 6.0) * v + (4.0 * al * al * r2 - 6.0 * al) * v_a;
+          int64_t k = ao_index[is];
+          for (int a = L; a >= 0; --a)
+            for (int b = L - a; b >= 0; --b, ++k) {
+              const int c = L - a - b;
+              const double f = ao_factor[k];
+              const double g0 = gbar[k], g1 = gbar[ao_num + k], g2 = gbar[2 * ao_num + k],
+                           g3 = gbar[3 * ao_num + k], g4 = gbar[4 * ao_num + k];
+              if (g0 == 0.0 && g1 == 0.0 && g2 == 0.0 && g3 == 0.0 && g4 == 0.0) continue;
+              const double gd[3] = {g1, g2, g3};
+              const double P = OR_D(P, 0, 0, 0);
+              const double Pj[3] = {OR_D(P, 1, 0, 0), OR_D(P, 0, 1, 0), OR_D(P, 0, 0, 1)};
+              double Pjd[3][3];
+              for (int j = 0; j < 3; ++j)
+                for (int d = 0; d < 3; ++d) {
+                  int e[3] = {0, 0, 0};
+                  e[j] += 1;
+                  e[d] += 1;
+                  Pjd[j][d] = OR_D(P, e[0], e[1], e[2]);
+                }
+              const double lapP = Pjd[0][0] + Pjd[1][1] + Pjd[2][2];
+              if (de) {
+                /* outputs of this primitive: phi = P v, d_d phi, lap phi; their exponent derivatives */
+                double s = g0 * P * v_a;
+                for (int d = 0; d < 3; ++d) s += gd[d] * (Pj[d] * v_a + P * dv_a[d]);
+                double lap_a = lapP * v_a + P * lapv_a;
+                for (int d = 0; d < 3; ++d) lap_a += 2.0 * Pj[d] * dv_a[d];
+                s += g4 * lap_a;
+                de[q] += f * s;
+              }
+              if (d_coord)
+                for (int j = 0; j < 3; ++j) {
+                  double dlapP = 0.0;
+                  for (int d = 0; d < 3; ++d) {
+                    int e[3] = {0, 0, 0};
+                    e[j] += 1;
+                    e[d] += 2;
+                    dlapP += OR_D(P, e[0], e[1], e[2]);
+                  }
+                  double s = g0 * (Pj[j] * v + P * dv[j]);
+                  for (int d = 0; d < 3; ++d)
+                    s += gd[d] * (Pjd[j][d] * v + Pj[d] * dv[j] + Pj[j] * dv[d] + P * d2v[j][d]);
+                  double t = dlapP * v + lapP * dv[j] + Pj[j] * lapv + P * dlapv[j];
+                  for (int d = 0; d < 3; ++d) t += 2.0 * (Pjd[d][j] * dv[d] + Pj[d] * d2v[d][j]);
+                  s += g4 * t;
+                  gc[j] += f * s;
+                }
+            }
+        }
+      }
+      if (d_coord)
+        for (int j = 0; j < 3; ++j) d_coord[p * 3 + j] = gc[j];
+    }
+    free(gbar);
+  }
+  if (d_coef) {
+    for (int64_t i = 0; i < mo_num * ao_num; ++i) {
+      double s = 0.0;
+      for (int t = 0; t < nthreads; ++t) s += dc_all[(size_t)t * (size_t)(mo_num * ao_num) + i];
+      d_coef[i] = s;
+    }
+  }
+  if (d_expo) {
+    for (int64_t q = 0; q < prim_num; ++q) {
+      double s = 0.0;
+      for (int t = 0; t < nthreads; ++t) s += de_all[(size_t)t * (size_t)prim_num + q];
+      d_expo[q] = s;
+    }
+  }
+  free(dc_all);
+  free(de_all);
+  free(s2n);
+  free(ao_index);
+  free(ao);
+  free(shell_vgl);
+  free(nucleus_prim_index);
+  free(coef_norm);
+  free(nmax);
+  free(nrange);
+  return 0;
+}
+#undef OR_D
