@@ -401,6 +401,30 @@ qmckl_exit_code_device qmckl_batch_autotune_device(qmckl_batch_device batch);
 /* Kernels launched by one provide (all stages). */
 int64_t qmckl_batch_get_launch_count_device(qmckl_batch_device batch);
 
+/* ---- Adjoint form: vector-Jacobian products (no counterpart in the reference) -------------
+ *
+ * For the scalar L = sum_{p,l,m} w[p][l][m] * mo_vgl[p][l][m] of the current points,
+ * qmckl_vjp_mo_vgl_device writes
+ *   d_coefficient [mo_num][ao_num]  dL/dC, in the layout of qmckl_set_mo_basis_coefficient_device
+ *   d_exponent    [prim_num]        dL/d(primitive exponent), the user's primitive order
+ *   d_coord       [point_num][3]    dL/d(point coordinates), the 'N' layout of qmckl_set_point_device
+ * (any of them may be NULL: not computed). w is [point_num][5][mo_num] (the mo_vgl layout).
+ * Computed in FP64 whatever the precision mode, with the shell radials recomputed (nothing is
+ * stored between forward and adjoint). The MO kernel's zero-value skip is a constant mask: an AO
+ * whose value is exactly zero at a point passes no gradient there; screening decisions are
+ * constants. Pointers may be device or host memory. Results are deterministic (fixed-order
+ * reductions). Sizes too small give QMCKL_INVALID_ARG_3/5/7/9_DEVICE, a NULL w
+ * QMCKL_INVALID_ARG_2_DEVICE.
+ *
+ * qmckl_vjp_ao_vgl_device is the same for L = sum ao_vgl_bar[p][l][k] * ao_vgl[p][l][k]
+ * (ao_vgl_bar [point_num][5][ao_num]; no mask): exponent and coordinate gradients. */
+qmckl_exit_code_device qmckl_vjp_mo_vgl_device(qmckl_context_device context, const double* w, int64_t w_size,
+                                               double* d_coefficient, int64_t d_coefficient_size, double* d_exponent,
+                                               int64_t d_exponent_size, double* d_coord, int64_t d_coord_size);
+qmckl_exit_code_device qmckl_vjp_ao_vgl_device(qmckl_context_device context, const double* ao_vgl_bar,
+                                               int64_t ao_vgl_bar_size, double* d_exponent, int64_t d_exponent_size,
+                                               double* d_coord, int64_t d_coord_size);
+
 /* Test hook for allocation failure handling: the n-th device allocation from now on
  * (n >= 1) fails as if cudaMalloc had failed; n = 0 disables the hook. */
 qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device context, int64_t n);

@@ -215,6 +215,39 @@ class Context:
     def set_precision(self, mode):
         self.call("set_precision_mode", int(mode))
 
+    def vjp_mo_vgl(self, w, want=("coef", "expo", "coord"), prim_num=None):
+        """Gradients of sum(w * mo_vgl) (w: [P][5][M] numpy): dict with 'coef' [M][A],
+        'expo' [prim_num], 'coord' [P][3] (host arrays passed to the C ABI)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        P = w.shape[0]
+        M, A = self.mo_num, self.ao_num
+        K = prim_num if prim_num is not None else self._num("get_ao_basis_prim_num")
+        out = {k: None for k in ("coef", "expo", "coord")}
+        if "coef" in want:
+            out["coef"] = np.empty((M, A))
+        if "expo" in want:
+            out["expo"] = np.empty(K)
+        if "coord" in want:
+            out["coord"] = np.empty((P, 3))
+
+        def arg(a):
+            return (a.ctypes.data_as(ctypes.c_void_p), a.size) if a is not None else (None, 0)
+
+        self.call("vjp_mo_vgl", w.ctypes.data_as(ctypes.c_void_p), w.size, *arg(out["coef"]), *arg(out["expo"]),
+                  *arg(out["coord"]))
+        return {k: v for k, v in out.items() if v is not None}
+
+    def vjp_ao_vgl(self, ao_bar, want=("expo", "coord"), prim_num=None):
+        ao_bar = np.ascontiguousarray(ao_bar, dtype=np.float64)
+        P = ao_bar.shape[0]
+        K = prim_num if prim_num is not None else self._num("get_ao_basis_prim_num")
+        e = np.empty(K) if "expo" in want else None
+        c = np.empty((P, 3)) if "coord" in want else None
+        self.call("vjp_ao_vgl", ao_bar.ctypes.data_as(ctypes.c_void_p), ao_bar.size,
+                  e.ctypes.data_as(ctypes.c_void_p) if e is not None else None, 0 if e is None else e.size,
+                  c.ctypes.data_as(ctypes.c_void_p) if c is not None else None, 0 if c is None else c.size)
+        return {k: v for k, v in (("expo", e), ("coord", c)) if v is not None}
+
     # ------------------------------------------------------------------ GB300 extensions
     def set_async(self, on):
         self.call("set_async", 1 if on else 0)

@@ -68,6 +68,7 @@ void free_tables(Ctx* ctx, AoTables& t) {
   dfree(ctx, t.ao_factor);
   dfree(ctx, t.shell_orig);
   dfree(ctx, t.shell_nucl);
+  dfree(ctx, t.prim_orig);
   dfree(ctx, t.chunks);
   dfree(ctx, t.exp_table);
   t.exp_table = nullptr;
@@ -75,7 +76,7 @@ void free_tables(Ctx* ctx, AoTables& t) {
   t.shells = nullptr;
   t.prims = nullptr;
   t.ao_factor = nullptr;
-  t.shell_orig = t.shell_nucl = nullptr;
+  t.shell_orig = t.shell_nucl = t.prim_orig = nullptr;
   t.chunks = nullptr;
   t.valid = false;
 }
@@ -137,6 +138,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   t.h_prims.clear();
   t.h_chunks.clear();
   t.h_shell_orig.clear();
+  t.h_prim_orig.clear();
   t.h_shell_nucl.clear();
   t.level_offsets.clear();
   t.level_sizes.clear();
@@ -168,6 +170,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
         pe.m2a = -2.0 * expo[p];
         pe.thr_bits = prim_threshold(expo[p]);
         t.h_prims.push_back(pe);
+        t.h_prim_orig.push_back((int32_t)p);
       }
       se.prim_end = (int32_t)t.h_prims.size();
       se.ao_begin = ao_counter;
@@ -239,10 +242,19 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   t.ao_factor = to_device(ctx, t.h_ao_factor);
   t.shell_orig = to_device(ctx, t.h_shell_orig);
   t.shell_nucl = to_device(ctx, t.h_shell_nucl);
+  t.prim_orig = to_device(ctx, t.h_prim_orig);
+  {
+    std::vector<char> seen((size_t)K, 0);
+    t.prims_unique = true;
+    for (int32_t q : t.h_prim_orig) {
+      if (seen[(size_t)q]) t.prims_unique = false;
+      seen[(size_t)q] = 1;
+    }
+  }
   t.chunks = to_device(ctx, t.h_chunks);
   t.exp_table = to_device(ctx, et);
   if (!t.nuclei || !t.shells || !t.prims || !t.ao_factor || !t.shell_orig || !t.shell_nucl || !t.chunks ||
-      !t.exp_table) {
+      !t.exp_table || (!t.h_prim_orig.empty() && !t.prim_orig)) {
     free_tables(ctx, t);
     return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "kernel tables");
   }

@@ -41,55 +41,18 @@
 #include <cstdint>
 
 #include "internal.hpp"
+#include "ao_device.cuh"
 
 namespace qg {
 namespace {
 
 constexpr int kWarps = 4;          // warps per CTA (each runs its own task)
-constexpr int kStage = 8;          // AOs staged per warp between flushes
-constexpr int kPad = 33;           // 32 points + 1 (bank-conflict padding), in doubles
-constexpr unsigned kFull = 0xffffffffu;
+using namespace dev;
 
 enum class Out { Vgl, Value, Planes };
 template <Out O>
 __host__ __device__ constexpr int ncomp() {
   return O == Out::Value ? 1 : 5;
-}
-
-template <int NC>
-struct Stage {
-  double v[NC][kStage][kPad];
-  int64_t pidx[32];  // point index of each lane (-1: no point)
-};
-
-__device__ __forceinline__ uint64_t bits_of(double x) { return static_cast<uint64_t>(__double_as_longlong(x)); }
-__device__ __forceinline__ bool is_one(double f) { return bits_of(f) == 0x3FF0000000000000ull; }
-
-// ---------------------------------------------------------------- exponential
-// e^(-x) for 0 <= x <= 27.7 (the screened range: fl(a r2) <= 27.631...), Tang's method:
-// x = (n/32) ln 2 + r with |r| <= ln2/64, e^-x = 2^(n>>5) * 2^((n&31)/32) * e^r.
-constexpr double kInvL = 46.166241308446828;               // 32 / ln 2 (only rounds n)
-constexpr double kShifter = 6755399441055744.0;            // 1.5 * 2^52: rounds to an integer
-constexpr double kL1 = 0.6931471805599453094 / 32.0;       // double nearest ln 2, / 32 (exact)
-constexpr double kL2 = 2.3190468138462996e-17 / 32.0;      // ln 2 - that double, / 32
-
-__device__ __forceinline__ double exp_neg(double x, const double* __restrict__ thi, const double* __restrict__ tlo) {
-  const double y = -x;
-  const double t = fma(y, kInvL, kShifter);
-  const int n = __double2loint(t);
-  const double nd = t - kShifter;
-  double r = fma(-nd, kL1, y);
-  r = fma(-nd, kL2, r);
-  double p = fma(r, 1.0 / 720.0, 1.0 / 120.0);
-  p = fma(p, r, 1.0 / 24.0);
-  p = fma(p, r, 1.0 / 6.0);
-  p = fma(p, r, 0.5);
-  p = fma(p, r, 1.0);
-  p = p * r;  // e^r - 1
-  const int j = n & 31, m = n >> 5;
-  const double th = thi[j];
-  const double res = fma(th, p, tlo[j]) + th;
-  return __longlong_as_double(__double_as_longlong(res) + ((long long)m << 52));
 }
 
 // ---------------------------------------------------------------- output staging
@@ -385,21 +348,13 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   w.flush();
 }
 
-// Loads the exponential's table into the first 512 bytes of dynamic shared memory.
-__device__ __forceinline__ void load_exp_table(const ExpTable* __restrict__ tab, double* thi, double* tlo) {
-  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
-    thi[i] = tab->hi[i];
-    tlo[i] = tab->lo[i];
-  }
-}
-
 // One molecule: warp task = blockIdx.x * kWarps + warp.
 template <Out O>
 __global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* thi = reinterpret_cast<double*>(smem_raw);
   double* tlo = thi + 32;
-  load_exp_table(a.exp_table, thi, tlo);
+  load_exp_table(a.exp_table->hi, a.exp_table->lo, thi, tlo);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
@@ -416,7 +371,7 @@ __global__ void __launch_bounds__(kWarps * 32) ao_batch_kernel(const FusedArgs* 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* thi = reinterpret_cast<double*>(smem_raw);
   double* tlo = thi + 32;
-  load_exp_table(mols[0].exp_table, thi, tlo);
+  load_exp_table(mols[0].exp_table->hi, mols[0].exp_table->lo, thi, tlo);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + 512) + warp;

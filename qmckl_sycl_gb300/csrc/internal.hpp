@@ -69,6 +69,8 @@ struct AoTables {
   double* ao_factor = nullptr;      // [ao_num]
   int32_t* shell_orig = nullptr;    // packed shell -> user shell index
   int32_t* shell_nucl = nullptr;    // packed shell -> nucleus
+  int32_t* prim_orig = nullptr;     // packed primitive -> user primitive index
+  bool prims_unique = true;         // no user primitive is shared by two shells
   NucleusChunk* chunks = nullptr;   // all chunk levels, concatenated
   // Level v splits the nuclei into level_sizes[v] chunks of balanced cost, stored at
   // chunks + level_offsets[v]; the launch picks the level that fills the GPU.
@@ -85,7 +87,7 @@ struct AoTables {
   std::vector<ShellEntry> h_shells;
   std::vector<PrimEntry> h_prims;
   std::vector<NucleusChunk> h_chunks;
-  std::vector<int32_t> h_shell_orig, h_shell_nucl;
+  std::vector<int32_t> h_shell_orig, h_shell_nucl, h_prim_orig;
   std::vector<double> h_ao_factor;
 };
 
@@ -221,6 +223,9 @@ struct qmckl_context_struct_device {
   // grow-only scratch for layout changes of host inputs (points, nuclei)
   void* staging = nullptr;
   size_t staging_cap = 0;
+  // grow-only scratch of the adjoint (vector-Jacobian) calls
+  void* vjp_buf = nullptr;
+  size_t vjp_cap = 0;
 
   // profiling
   bool profiling = false;
@@ -298,6 +303,13 @@ cudaError_t launch_mo_vgl_fp64(Ctx* ctx, const double* ao_vgl, const double* coe
 cudaError_t launch_mo_value_fp64(Ctx* ctx, const double* ao_value, const double* coef_t, int64_t point_num,
                                  int64_t ao_num, int64_t mo_num, double* mo_value);
 cudaError_t launch_transpose(Ctx* ctx, const double* in, int64_t rows, int64_t cols, double* out);
+// Plain row-major FP64 products on the DMMA pipe: C[R][N] = A[R][K] * B[K][N]; the split-K form
+// sums nparts K-slices (parts: nparts x R x N scratch) in a fixed order.
+cudaError_t launch_dgemm_rm(Ctx* ctx, const double* A, const double* B, double* C, int64_t R, int64_t K, int64_t N,
+                            const char* name);
+int64_t dgemm_splitk_parts(int64_t R, int64_t K, int64_t N, int sms);
+cudaError_t launch_dgemm_splitk(Ctx* ctx, const double* A, const double* B, double* parts, int64_t nparts, double* C,
+                                int64_t R, int64_t K, int64_t N, const char* name);
 
 // ---- multi-molecule (batched) launches: one launch covers the work of every molecule ----
 // Arguments of the fused AO kernel for one molecule (one warp task = 32 points x one

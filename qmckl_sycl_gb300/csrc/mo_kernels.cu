@@ -33,24 +33,26 @@ __device__ __forceinline__ void dmma_16x8x4(double (&d)[4], double a0, double a1
 // Element (r, k) of A (row-major, ld = K) with bounds and, when MASK, the reference's
 // zero-value skip for rows whose component (r % 5) is not 0.
 template <bool MASK>
-__device__ __forceinline__ double load_a(const double* __restrict__ A, int64_t R, int64_t K, int64_t r, int64_t k) {
+__device__ __forceinline__ double load_a(const double* __restrict__ A, int64_t lda, int64_t R, int64_t K, int64_t r,
+                                         int64_t k) {
   if (r >= R || k >= K) return 0.0;
-  double v = __ldg(A + r * K + k);
+  double v = __ldg(A + r * lda + k);
   if constexpr (MASK) {
     const int comp = (int)(r % 5);
     if (comp != 0) {
-      const double v0 = __ldg(A + (r - comp) * K + k);
+      const double v0 = __ldg(A + (r - comp) * lda + k);
       if (v0 == 0.0) v = 0.0;
     }
   }
   return v;
 }
 
-// One warp's 32x32 tile of C at (r0, c0), if it starts inside C.
+// One warp's 32x32 tile of C at (r0, c0), if it starts inside C. A is R x K with leading
+// dimension lda (lda > K for a K-slice of a wider matrix), B is K x N, C is R x N.
 template <bool MASK>
-__device__ __forceinline__ void dgemm_warp_tile(const double* __restrict__ A, const double* __restrict__ B,
-                                                double* __restrict__ C, int64_t R, int64_t K, int64_t N, int64_t r0,
-                                                int64_t c0, int lane) {
+__device__ __forceinline__ void dgemm_warp_tile(const double* __restrict__ A, int64_t lda,
+                                                const double* __restrict__ B, double* __restrict__ C, int64_t R,
+                                                int64_t K, int64_t N, int64_t r0, int64_t c0, int lane) {
   if (r0 >= R || c0 >= N) return;  // warp-uniform
   const int g = lane >> 2, t = lane & 3;
   double acc[2][4][4];
@@ -70,8 +72,8 @@ __device__ __forceinline__ void dgemm_warp_tile(const double* __restrict__ A, co
     double a[2][2], b[4];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
-      a[i][0] = load_a<MASK>(A, R, K, r0 + 16 * i + g, k + t);
-      a[i][1] = load_a<MASK>(A, R, K, r0 + 16 * i + g + 8, k + t);
+      a[i][0] = load_a<MASK>(A, lda, R, K, r0 + 16 * i + g, k + t);
+      a[i][1] = load_a<MASK>(A, lda, R, K, r0 + 16 * i + g + 8, k + t);
     }
     const bool kok = k + t < K;
 #pragma unroll
@@ -103,7 +105,28 @@ __global__ void __launch_bounds__(128) dgemm_dmma_kernel(const double* __restric
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
   const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
-  dgemm_warp_tile<MASK>(A, B, C, R, K, N, r0, c0, lane);
+  dgemm_warp_tile<MASK>(A, K, B, C, R, K, N, r0, c0, lane);
+}
+
+// Split-K: CTA z computes the K-slice [z*kc, min(K, (z+1)*kc)) of A*B into parts[z] (R x N).
+__global__ void __launch_bounds__(128) dgemm_splitk_kernel(const double* __restrict__ A, const double* __restrict__ B,
+                                                           double* __restrict__ parts, int64_t R, int64_t K,
+                                                           int64_t N, int64_t kc) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t k0 = (int64_t)blockIdx.z * kc;
+  const int64_t kn = (K - k0) < kc ? (K - k0) : kc;
+  const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
+  const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
+  dgemm_warp_tile<false>(A + k0, K, B + k0 * N, parts + (int64_t)blockIdx.z * R * N, R, kn, N, r0, c0, lane);
+}
+
+// out[i] = sum over z (in order) of parts[z][i].
+__global__ void sum_parts_kernel(const double* __restrict__ parts, int nparts, int64_t n, double* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double s = 0.0;
+  for (int z = 0; z < nparts; ++z) s += parts[(int64_t)z * n + i];
+  out[i] = s;
 }
 
 // Several contractions, persistent: a CTA of WR x WC warps owns (32 WR) x (32 WC) tiles of C,
@@ -130,7 +153,7 @@ __global__ void __launch_bounds__(32 * WR * WC) dgemm_batch_kernel(const GemmJob
     const int local = tile - tile_begin[lo];
     const int64_t r0 = (int64_t)(local / jb.col_tiles) * (32 * WR) + (warp / WC) * 32;
     const int64_t c0 = (int64_t)(local % jb.col_tiles) * (32 * WC) + (warp % WC) * 32;
-    dgemm_warp_tile<MASK>(jb.a, jb.b, jb.c, jb.rows, jb.k, jb.cols, r0, c0, lane);
+    dgemm_warp_tile<MASK>(jb.a, jb.k, jb.b, jb.c, jb.rows, jb.k, jb.cols, r0, c0, lane);
   }
 }
 
@@ -179,6 +202,36 @@ cudaError_t launch_dgemm_batch(cudaStream_t stream, int shape, bool mask5, const
     case 5: return launch_batch_shape<true, 2, 4>(stream, jobs, tile_begin, njobs, total_tiles, counter);
     default: return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_dgemm_rm(Ctx* ctx, const double* A, const double* B, double* C, int64_t R, int64_t K, int64_t N,
+                            const char* name) {
+  return launch_dgemm<false>(ctx, A, B, C, R, K, N, name);
+}
+
+int64_t dgemm_splitk_parts(int64_t R, int64_t K, int64_t N, int sms) {
+  const int64_t tiles = ((R + kCM - 1) / kCM) * ((N + kCN - 1) / kCN);
+  int64_t z = (4 * (int64_t)sms + tiles - 1) / tiles;  // about four CTAs per SM
+  const int64_t max_by_k = (K + 63) / 64;               // slices of at least 64
+  if (z > max_by_k) z = max_by_k;
+  return z < 1 ? 1 : z;
+}
+
+cudaError_t launch_dgemm_splitk(Ctx* ctx, const double* A, const double* B, double* parts, int64_t nparts, double* C,
+                                int64_t R, int64_t K, int64_t N, const char* name) {
+  if (R <= 0 || N <= 0) return cudaSuccess;
+  if (K <= 0 || nparts < 1) return cudaMemsetAsync(C, 0, sizeof(double) * R * N, ctx->stream);
+  int64_t kc = (K + nparts - 1) / nparts;
+  kc = (kc + 3) / 4 * 4;
+  const int64_t z = (K + kc - 1) / kc;
+  dim3 grid((unsigned)((N + kCN - 1) / kCN), (unsigned)((R + kCM - 1) / kCM), (unsigned)z);
+  {
+    LaunchScope scope(ctx, name);
+    dgemm_splitk_kernel<<<grid, 128, 0, ctx->stream>>>(A, B, parts, R, K, N, kc);
+  }
+  LaunchScope scope(ctx, "sum_parts");
+  sum_parts_kernel<<<(unsigned)((R * N + 255) / 256), 256, 0, ctx->stream>>>(parts, (int)z, R * N, C);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_mo_vgl_fp64(Ctx* ctx, const double* ao_vgl, const double* coef_t, int64_t point_num,
