@@ -374,6 +374,63 @@ def time_batched(dist, steps, warmup, peaks, fp64_peak):
     return out
 
 
+def time_adjoint(dist, steps, warmup, fp64_peak):
+    """The adjoint form on its workload (8 nuclei, ~200 AOs, 64 MOs, 2048 points): one step =
+    new points + qmckl_vjp_mo_vgl_device for all three gradients (coefficients, exponents,
+    coordinates), W ~ N(0, 1) resident on the device."""
+    from qmckl_sycl_gb300 import Context, config_adjoint
+
+    sy = config_adjoint(0)
+    P, A, M, K = sy.point_num, sy.ao_num, sy.mo_num, sy.prim_num
+    ctx = Context(dist.local_rank)
+    ctx.load_system(sy)
+    w = np.random.default_rng(5).normal(size=(P, 5, M))
+    wd = ctx.upload(w)
+    dc = ctx.buffer("dc", 8 * M * A)
+    de = ctx.buffer("de", 8 * K)
+    dx = ctx.buffer("dx", 8 * 3 * P)
+
+    def step():
+        ctx.touch()
+        ctx.call("vjp_mo_vgl", wd.ptr, w.size, dc.ptr, M * A, de.ptr, K, dx.ptr, 3 * P)
+
+    ctx.set_async(True)
+    for _ in range(warmup):
+        step()
+    ctx.synchronize()
+    dist.barrier()
+    reps = max(steps, 20)
+    ctx.call("timer_start")
+    for _ in range(reps):
+        step()
+    ms = ctypes.c_double(0)
+    ctx.call("timer_stop", ctypes.byref(ms))
+    ctx.synchronize()
+    ctx.set_async(False)
+    t = dist.max(ms.value) / reps
+    ctx.set_profiling(True)
+    ctx.reset_kernel_stats()
+    for _ in range(3):
+        step()
+    stats = ctx.kernel_stats()
+    ctx.close()
+    kern = {}
+    gemm_flops = 2.0 * 5 * P * M * A
+    for k, (n, tot) in stats.items():
+        if n <= 0:
+            continue
+        kms = tot / n
+        kern[k] = {"ms_per_launch": kms, "launches_per_step": n / 3.0}
+        if k in ("vjp_ao_adjoint_dgemm", "vjp_coefficient_dgemm"):
+            kern[k].update({"bound": "tensor", "achieved": gemm_flops / (kms * 1e-3) / 1e12, "peak": fp64_peak,
+                            "unit": "TFLOP/s"})
+            kern[k]["frac"] = kern[k]["achieved"] / fp64_peak
+    return {"workload": "adjoint: %d nuclei, %d shells, %d primitives, %d AOs, %d MOs, %d points; L = sum(W * mo_vgl), "
+                        "W ~ N(0,1); gradients w.r.t. C, exponents, coordinates (FP64)" % (
+                            sy.nucl_num, sy.shell_num, K, A, M, P),
+            "value": dist.sum(P) / (t * 1e-3), "unit": "points/s", "ms_per_step": t, "kernels": kern}
+
+
 def main():
     args = parse()
     dist = Dist()
@@ -468,6 +525,7 @@ def main():
         v, cores, sample = cpu_baseline(s, args.cpu_seconds)
         cpu = {"value": v, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample}
 
+    adj = time_adjoint(dist, args.steps, args.warmup, fp64_peak.value)
     bt = None
     if not args.no_batched:
         bt = time_batched(dist, args.steps, args.warmup, peaks, fp64_peak.value)
@@ -491,6 +549,7 @@ def main():
     if acc:
         line["mixed_vs_fp64_error"] = acc
         line["mixed_over_fp64"] = results["mixed"]["value"] / results["fp64"]["value"]
+    line["adjoint"] = adj
     if bt:
         line["batched"] = bt
     print(json.dumps(line), flush=True)

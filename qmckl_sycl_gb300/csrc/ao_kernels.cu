@@ -56,7 +56,35 @@ __host__ __device__ constexpr int ncomp() {
 }
 
 // ---------------------------------------------------------------- output staging
-// Collects one warp's AO values (lane = point) and writes them as row segments.
+// Splits an FP64 value into three BF16 terms (hi + mid + lo carries 24 significant bits) with
+// integer and FP32 instructions only: FP64 -> FP32 by round-to-nearest-even on the bit pattern
+// (values below the FP32 normal range become zero, which is below the form's error budget).
+__device__ __forceinline__ void split_bf16x3(double a, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7FF) - 896;
+  float f;
+  if (e <= 0) {
+    f = __uint_as_float(sign);
+  } else {
+    const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+    const unsigned int mm = (unsigned int)(frac >> 29);
+    const unsigned long long rem = frac & 0x1FFFFFFFull;
+    unsigned int bits = ((unsigned int)(e < 255 ? e : 255) << 23) | (e < 255 ? mm : 0u);
+    if (e < 255 && (rem > 0x10000000ull || (rem == 0x10000000ull && (mm & 1u)))) bits += 1u;
+    f = __uint_as_float(sign | bits);
+  }
+  h = __float2bfloat16_rn(f);
+  const float r1 = f - __bfloat162float(h);
+  m = __float2bfloat16_rn(r1);
+  l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+}
+
+// Collects one warp's AO values (lane = point) and writes them as row segments. Windows of
+// kStage AOs are aligned to multiples of kStage (the first window of a task may be shorter):
+// when the row length is a multiple of 4, a full window of ao_vgl then covers whole 32-byte
+// sectors, which saves the memory system a read-modify-write per row (17 % of the FP64 AO
+// kernel's time on the medium workload).
 template <Out O>
 struct Writer {
   static constexpr int NC = ncomp<O>();
@@ -69,6 +97,7 @@ struct Writer {
   int lane;
   int base;                  // AO index of stage slot 0
   int fill;                  // staged AOs
+  int cap;                   // capacity of the current window
 
   __device__ __forceinline__ void flush() {
     __syncwarp();
@@ -82,29 +111,9 @@ struct Writer {
       const int64_t pt = st->pidx[q];
       const double val = st->v[c][j][q];
       if constexpr (O == Out::Planes) {
-        // the reference's MO kernel drops an AO whose value is exactly zero from every
-        // component of the point (src/qmckl_mo_sycl.cpp:40)
-        const double a = (c != 0 && st->v[0][j][q] == 0.0) ? 0.0 : val;
         const int64_t o = (5 * pt + c) * row_len + base + j;
-        // split into three BF16 terms with integer and FP32 instructions (no FP64)
-        const unsigned long long b = (unsigned long long)__double_as_longlong(a);
-        const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-        const int e = (int)((b >> 52) & 0x7FF) - 896;
-        float f;
-        if (e <= 0) {
-          f = __uint_as_float(sign);
-        } else {
-          const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
-          const unsigned int mm = (unsigned int)(frac >> 29);
-          const unsigned long long rem = frac & 0x1FFFFFFFull;
-          unsigned int bits = ((unsigned int)(e < 255 ? e : 255) << 23) | (e < 255 ? mm : 0u);
-          if (e < 255 && (rem > 0x10000000ull || (rem == 0x10000000ull && (mm & 1u)))) bits += 1u;
-          f = __uint_as_float(sign | bits);
-        }
-        const __nv_bfloat16 h = __float2bfloat16_rn(f);
-        const float r1 = f - __bfloat162float(h);
-        const __nv_bfloat16 md = __float2bfloat16_rn(r1);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(md));
+        __nv_bfloat16 h, md, lo;
+        split_bf16x3(val, h, md, lo);
         planes[o] = h;
         planes[plane_stride + o] = md;
         planes[2 * plane_stride + o] = lo;
@@ -115,11 +124,22 @@ struct Writer {
     __syncwarp();
     base += fill;
     fill = 0;
+    cap = kStage;
   }
   __device__ __forceinline__ void emit(const double (&v)[NC]) {
-    if (fill == kStage) flush();
+    if (fill == cap) flush();
+    if constexpr (O == Out::Planes) {
+      // the reference's MO kernel drops an AO whose value is exactly zero from every
+      // component of the point (src/qmckl_mo_sycl.cpp:40); tested on the bit pattern (+-0),
+      // which keeps the FP64 pipe free
+      const bool drop = (bits_of(v[0]) << 1) == 0;
+      st->v[0][fill][lane] = v[0];
 #pragma unroll
-    for (int c = 0; c < NC; ++c) st->v[c][fill][lane] = v[c];
+      for (int c = 1; c < NC; ++c) st->v[c][fill][lane] = drop ? 0.0 : v[c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) st->v[c][fill][lane] = v[c];
+    }
     fill += 1;
   }
   __device__ __forceinline__ void emit_zeros(int count) {
@@ -280,6 +300,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   const NucleusChunk cj = a.chunks[ch];
   w.base = cj.ao_begin;
   w.fill = 0;
+  w.cap = kStage - (cj.ao_begin & (kStage - 1));
 
   for (int n = cj.nucl_begin; n < cj.nucl_end; ++n) {
     const NucleusEntry& N = a.nuclei[n];
