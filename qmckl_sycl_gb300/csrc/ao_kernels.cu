@@ -80,7 +80,8 @@ __device__ __forceinline__ void split_bf16x3(double a, __nv_bfloat16& h, __nv_bf
   l = __float2bfloat16_rn(r1 - __bfloat162float(m));
 }
 
-// Collects one warp's AO values (lane = point) and writes them as row segments. Windows of
+// Collects one warp's AO values (lane = point) for ao_vgl / ao_value and writes them as row
+// segments (lanes hold scattered points, so rows are staged in shared memory). Windows of
 // kStage AOs are aligned to multiples of kStage (the first window of a task may be shorter):
 // when the row length is a multiple of 4, a full window of ao_vgl then covers whole 32-byte
 // sectors, which saves the memory system a read-modify-write per row (17 % of the FP64 AO
@@ -89,10 +90,8 @@ template <Out O>
 struct Writer {
   static constexpr int NC = ncomp<O>();
   Stage<NC>* st;
-  double* out;               // ao_vgl / ao_value (Vgl, Value)
-  __nv_bfloat16* planes;     // Planes: [3][5P][row_len]
-  int64_t plane_stride;      // Planes: 5P * row_len
-  int64_t row_len;           // ao_num, or kp for Planes
+  double* out;               // ao_vgl / ao_value
+  int64_t row_len;           // ao_num
   int nvalid;                // points of the warp that exist
   int lane;
   int base;                  // AO index of stage slot 0
@@ -110,16 +109,7 @@ struct Writer {
       if (j >= fill) continue;
       const int64_t pt = st->pidx[q];
       const double val = st->v[c][j][q];
-      if constexpr (O == Out::Planes) {
-        const int64_t o = (5 * pt + c) * row_len + base + j;
-        __nv_bfloat16 h, md, lo;
-        split_bf16x3(val, h, md, lo);
-        planes[o] = h;
-        planes[plane_stride + o] = md;
-        planes[2 * plane_stride + o] = lo;
-      } else {
-        out[pt * (NC * row_len) + c * row_len + base + j] = val;
-      }
+      out[pt * (NC * row_len) + c * row_len + base + j] = val;
     }
     __syncwarp();
     base += fill;
@@ -128,24 +118,64 @@ struct Writer {
   }
   __device__ __forceinline__ void emit(const double (&v)[NC]) {
     if (fill == cap) flush();
-    if constexpr (O == Out::Planes) {
-      // the reference's MO kernel drops an AO whose value is exactly zero from every
-      // component of the point (src/qmckl_mo_sycl.cpp:40); tested on the bit pattern (+-0),
-      // which keeps the FP64 pipe free
-      const bool drop = (bits_of(v[0]) << 1) == 0;
-      st->v[0][fill][lane] = v[0];
 #pragma unroll
-      for (int c = 1; c < NC; ++c) st->v[c][fill][lane] = drop ? 0.0 : v[c];
-    } else {
-#pragma unroll
-      for (int c = 0; c < NC; ++c) st->v[c][fill][lane] = v[c];
-    }
+    for (int c = 0; c < NC; ++c) st->v[c][fill][lane] = v[c];
     fill += 1;
   }
   __device__ __forceinline__ void emit_zeros(int count) {
     double z[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) z[c] = 0.0;
+    for (int i = 0; i < count; ++i) emit(z);
+  }
+};
+
+// The split-BF16 form's AO operand, written M-major straight from registers: plane p, AO k,
+// operand row c * pp + s (component c of the point at processing slot s) at
+// planes[(p * kp + k) * 5 pp + c * pp + s]. The 32 lanes of a warp hold 32 consecutive slots,
+// so every store of the warp fills 64 contiguous bytes (two whole sectors) and nothing is
+// staged in shared memory. Slots past the last point (padding rows) are not written; the
+// contraction discards their rows.
+template <>
+struct Writer<Out::Planes> {
+  static constexpr int NC = 5;
+  Stage<5>* st;              // unused
+  double* out;               // unused
+  __nv_bfloat16* planes;
+  int64_t plane_stride;      // kp * 5 pp
+  int64_t row_len;           // 5 pp (elements per AO row)
+  int64_t pp;
+  int64_t slot;              // this lane's processing slot
+  int nvalid;
+  int lane;
+  int base;                  // AO index of the next emit
+  int fill;
+  int cap;
+
+  __device__ __forceinline__ void flush() {
+    base += fill;
+    fill = 0;
+  }
+  __device__ __forceinline__ void emit(const double (&v)[NC]) {
+    if (lane < nvalid) {
+      // the reference's MO kernel drops an AO whose value is exactly zero from every
+      // component of the point (src/qmckl_mo_sycl.cpp:40); tested on the bit pattern (+-0),
+      // which keeps the FP64 pipe free
+      const bool drop = (bits_of(v[0]) << 1) == 0;
+      __nv_bfloat16* o = planes + (int64_t)(base + fill) * row_len + slot;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        __nv_bfloat16 h, m, l;
+        split_bf16x3(c > 0 && drop ? 0.0 : v[c], h, m, l);
+        o[c * pp] = h;
+        o[plane_stride + c * pp] = m;
+        o[2 * plane_stride + c * pp] = l;
+      }
+    }
+    fill += 1;
+  }
+  __device__ __forceinline__ void emit_zeros(int count) {
+    const double z[NC] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int i = 0; i < count; ++i) emit(z);
   }
 };
@@ -291,12 +321,18 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   Writer<O> w;
   w.st = st;
   w.out = a.out;
-  w.planes = static_cast<__nv_bfloat16*>(a.planes);
-  w.plane_stride = 5 * P * a.row_len;
-  w.row_len = a.row_len;
+  if constexpr (O == Out::Planes) {
+    w.planes = static_cast<__nv_bfloat16*>(a.planes);
+    w.pp = a.plane_pp;
+    w.row_len = 5 * a.plane_pp;
+    w.plane_stride = a.row_len * 5 * a.plane_pp;
+    w.slot = p0 + lane;
+  } else {
+    w.row_len = a.row_len;
+    w.st->pidx[lane] = p;
+  }
   w.nvalid = nvalid;
   w.lane = lane;
-  w.st->pidx[lane] = p;
   const NucleusChunk cj = a.chunks[ch];
   w.base = cj.ao_begin;
   w.fill = 0;
@@ -518,7 +554,7 @@ int pick_level(const AoTables& t, int64_t groups, int sms) {
 
 template <Out O>
 size_t fused_smem() {
-  return 512 + sizeof(Stage<ncomp<O>()>) * kWarps;
+  return O == Out::Planes ? 512 : 512 + sizeof(Stage<ncomp<O>()>) * kWarps;
 }
 
 template <Out O>
@@ -604,6 +640,7 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.point_num = point_num;
   a.ao_num = t.ao_num;
   a.row_len = row_len;
+  a.plane_pp = (point_num + 31) / 32 * 32;
   a.task_num = ((point_num + 31) / 32) * a.chunk_num;
   return a;
 }

@@ -290,8 +290,10 @@ cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, cons
                           double* ao_vgl);
 cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
                             int64_t point_num, double* ao_value);
-// AO vgl written straight as the three BF16 planes of the split-BF16 contraction, planes
-// [3][5P][kp] (columns [ao_num, kp) zero), with the reference's zero-value skip applied.
+// AO vgl written straight as the three BF16 planes of the split-BF16 contraction, M-major:
+// planes [3][kp][5 pp] with pp = point_num rounded up to 32, operand row c * pp + s holding
+// component c of the point at processing slot s (perm order); AOs [ao_num, kp) are zero and
+// the reference's zero-value skip is applied.
 cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
                              int64_t point_num, int64_t kp, void* planes);
 cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num,
@@ -324,10 +326,11 @@ struct FusedArgs {
   const double* coord;      // [3][P]
   const int32_t* perm;      // processing order of the points, or null
   double* out;              // ao_vgl (FP64 output)
-  void* planes;             // BF16 planes [3][5P][row_len] (split-BF16 output)
+  void* planes;             // BF16 planes [3][row_len][5 plane_pp], M-major (split-BF16 output)
   int64_t point_num;
   int64_t ao_num;
   int64_t row_len;          // ao_num, or the padded K of the planes
+  int64_t plane_pp;         // points rounded up to a multiple of 32
   int64_t task_num;
   int chunk_num;
 };
@@ -376,6 +379,10 @@ size_t split_job_bytes();
 // job_host with column tiles of at most n_cap (16..96) columns; returns its tile count or -1.
 int split_make_job(void* job_host, const void* a_planes, int64_t rows, const void* b_planes, int64_t M, int64_t kp,
                    double* out, int tile_begin, int n_cap);
+// The same from the fused AO kernel's M-major planes ([3][kp][5 pp]; see launch_ao_planes) into
+// out[5 npts][M], operand row c * pp + s landing in output row 5 perm[s] + c.
+int split_make_job_mn(void* job_host, const void* a_planes, int64_t pp, int64_t npts, const int32_t* perm,
+                      const void* b_planes, int64_t M, int64_t kp, double* out, int tile_begin, int n_cap);
 cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, int total_tiles, int* err);
 int64_t split_k_pad(int64_t ao_num);
 // The member's coefficient planes for the split-BF16 form (built once per coefficient set)

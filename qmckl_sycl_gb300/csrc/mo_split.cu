@@ -157,6 +157,19 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   return d;
 }
 
+// Shared-memory descriptor of an M-major ("MN-major") operand tile with 128-byte swizzle, the
+// layout TMA writes for boxes of 64 M x 64 K: K rows of 128 bytes (64 consecutive M), 8-row
+// groups 1024 bytes apart (stride byte offset), and the second 64-wide M half 8 KB further
+// (leading byte offset).
+__device__ __forceinline__ uint64_t sdesc_mn(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(8192 >> 4) << 16;  // leading byte offset: next 64-element M block
+  d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: next 8-row K group
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
 __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
@@ -184,7 +197,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 // global memory so that one persistent launch can work through the tiles of many of them;
 // tile t of the launch belongs to the job with the largest tile_begin <= t.
 struct alignas(64) SplitJob {
-  CUtensorMap ta[3];  // A planes [3][rows][kp]
+  CUtensorMap ta[3];  // A planes: [3][rows][kp] (K-major) or [3][kp][rows] (M-major)
   CUtensorMap tb[3];  // B planes [3][cols][kp]
   double* out;        // [rows][ldo]
   int64_t rows;       // valid rows
@@ -194,6 +207,12 @@ struct alignas(64) SplitJob {
   int32_t n_tile;     // columns per tile (multiple of 16, <= kMaxN)
   int32_t col_tiles;  // tiles along the columns
   int32_t tile_begin; // index of this job's first tile in the launch
+  // M-major A (the fused AO kernel's plane layout): operand row r = c * pp + s is component c
+  // of the point at processing slot s; it lands in output row 5 * perm[s] + c (s < npts).
+  int32_t a_mn;
+  int32_t pp;         // points padded to a multiple of 32 (rows = 5 pp)
+  int64_t npts;
+  const int32_t* perm;  // processing order (null: identity)
 };
 
 // Correction terms (A plane, B plane): hi*mid, mid*hi, hi*lo, mid*mid, lo*hi.
@@ -316,7 +335,15 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
           unsigned char* st = base + s2 * stage_bytes;
           mbar_expect_tx(&full[s2], stage_bytes);
-          for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, &job.ta[i], kb * kBK, m0, &full[s2]);
+          if (job.a_mn) {
+            // two 64(M) x 64(K) boxes per plane: M rows m0..m0+63, then m0+64..m0+127
+            for (int i = 0; i < 3; ++i) {
+              tma_load_2d(st + i * kPlaneA, &job.ta[i], m0, kb * kBK, &full[s2]);
+              tma_load_2d(st + i * kPlaneA + kPlaneA / 2, &job.ta[i], m0 + 64, kb * kBK, &full[s2]);
+            }
+          } else {
+            for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, &job.ta[i], kb * kBK, m0, &full[s2]);
+          }
           for (int i = 0; i < 3; ++i) tma_load_2d(st + 3 * kPlaneA + i * plane_b, &job.tb[i], kb * kBK, n0, &full[s2]);
           issued = kb + 1;
         }
@@ -328,8 +355,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     } else if (warp == 1) {
       if (lane == 0) {
-        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
-                               ((uint32_t)(kBM >> 4) << 24);
+        // D = F32 (bit 4), A = B = BF16 (bits 7, 10), A M-major (bit 15) when a_mn, N >> 3, M >> 4
+        const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((job.a_mn ? 1u : 0u) << 15) |
+                               ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+        const bool amn = job.a_mn != 0;
         for (int kb = 0; kb < job.kblocks; ++kb) {
           const int s2 = kb % kStages, b = kb & 1, use = kb >> 1;
           const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
@@ -347,10 +376,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           const uint32_t main_acc = tmem + (uint32_t)((1 + b) * N);
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
-            umma_bf16(main_acc, sdesc(sa + kk * 32), sdesc(sb + kk * 32), idesc, kk > 0 ? 1u : 0u);
+            // a K step of 16: 32 bytes along a K-major row, or 16 rows of 128 bytes (M-major)
+            const uint64_t a0 = amn ? sdesc_mn(sa + kk * 2048) : sdesc(sa + kk * 32);
+            umma_bf16(main_acc, a0, sdesc(sb + kk * 32), idesc, kk > 0 ? 1u : 0u);
 #pragma unroll
             for (int t = 0; t < 5; ++t) {
-              const uint64_t ad = sdesc(sa + kPairA[t] * kPlaneA + kk * 32);
+              const uint32_t aa = sa + kPairA[t] * kPlaneA;
+              const uint64_t ad = amn ? sdesc_mn(aa + kk * 2048) : sdesc(aa + kk * 32);
               const uint64_t bd = sdesc(sb + kPairB[t] * plane_b + kk * 32);
               umma_bf16(tmem, ad, bd, idesc, (kb | kk | t) != 0);
             }
@@ -410,8 +442,13 @@ __global__ void __launch_bounds__(kThreads, 1)
           tmem_ld16(lb + (uint32_t)c0, c);
           tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
           tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
-          if (row < job.rows) {
-            double* o = job.out + row * job.ldo + n0 + c0;
+          int64_t orow = row < job.rows ? row : -1;
+          if (job.a_mn && orow >= 0) {
+            const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+            orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
+          }
+          if (orow >= 0) {
+            double* o = job.out + orow * job.ldo + n0 + c0;
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               float s2, e2;
@@ -473,6 +510,20 @@ bool encode_map(CUtensorMap* map, const void* base, int64_t rows, int64_t kp, in
   return r == CUDA_SUCCESS;
 }
 
+// M-major A plane [kp][rows]: boxes of 64 rows (inner, 128 bytes) x 64 K.
+bool encode_map_mn(CUtensorMap* map, const void* base, int64_t rows, int64_t kp) {
+  EncodeTiledFn encode = encode_tiled_fn();
+  if (!encode) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)rows, (cuuint64_t)kp};
+  cuuint64_t strides[1] = {(cuuint64_t)rows * 2};
+  cuuint32_t box[2] = {64, (cuuint32_t)kBK};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 // Column tiling of an M-column contraction: the fewest tiles of at most kMaxN columns,
@@ -501,6 +552,32 @@ int make_job(SplitJob& job, const __nv_bfloat16* ap, int64_t rows, const __nv_bf
   job.n_tile = n_tile;
   job.col_tiles = (int32_t)((M + n_tile - 1) / n_tile);
   job.tile_begin = tile_begin;
+  return (int)((rows + kBM - 1) / kBM) * job.col_tiles;
+}
+
+// The mo_vgl contraction from the fused AO kernel's M-major planes ap ([3][kp][5 pp], row
+// c * pp + s = component c of processing slot s) into out[5 npts][M] (rows 5 perm[s] + c).
+int make_job_mn(SplitJob& job, const __nv_bfloat16* ap, int64_t pp, int64_t npts, const int32_t* perm,
+                const __nv_bfloat16* bp, int64_t M, int64_t kp, double* out, int tile_begin, int n_cap = kMaxN) {
+  memset(&job, 0, sizeof job);
+  const int n_tile = tile_cols(M, n_cap);
+  const int64_t rows = 5 * pp;
+  for (int i = 0; i < 3; ++i)
+    if (!encode_map_mn(&job.ta[i], ap + (size_t)i * kp * rows, rows, kp) ||
+        !encode_map(&job.tb[i], bp + (size_t)i * M * kp, M, kp, n_tile))
+      return -1;
+  job.out = out;
+  job.rows = rows;
+  job.cols = M;
+  job.ldo = M;
+  job.kblocks = (int32_t)(kp / kBK);
+  job.n_tile = n_tile;
+  job.col_tiles = (int32_t)((M + n_tile - 1) / n_tile);
+  job.tile_begin = tile_begin;
+  job.a_mn = 1;
+  job.pp = (int32_t)pp;
+  job.npts = npts;
+  job.perm = perm;
   return (int)((rows + kBM - 1) / kBM) * job.col_tiles;
 }
 
@@ -546,14 +623,11 @@ static qmckl_exit_code_device ensure_coef_planes(Ctx* ctx, qmckl_context_device 
   return finish(ctx, c, "qmckl_provide_mo_basis_mo_vgl_device");
 }
 
-// out[rows][M] = split-BF16 product of the A planes ap ([3][rows][kp]) and the coefficients.
-static qmckl_exit_code_device contract_planes(Ctx* ctx, qmckl_context_device c, const __nv_bfloat16* ap, int64_t rows,
-                                              int64_t kp, int* err, double* out, const char* name) {
+// Uploads one job and runs its tiles on the context's stream.
+static qmckl_exit_code_device run_job(Ctx* ctx, qmckl_context_device c, const SplitJob& job, int tiles, int* err,
+                                      const char* name) {
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
   MoBasisData& mo = ctx->mo_basis;
-  SplitJob job;
-  const int tiles =
-      make_job(job, ap, rows, static_cast<const __nv_bfloat16*>(mo.coef_split), mo.mo_num, kp, out, 0);
   if (tiles < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
   if (!ensure_raw(ctx, &mo.split_job, &mo.split_job_cap, sizeof(SplitJob)))
     return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptor");
@@ -573,6 +647,16 @@ static qmckl_exit_code_device contract_planes(Ctx* ctx, qmckl_context_device c, 
     if (h) return fail(c, QMCKL_FAILURE_DEVICE, fn, "split-BF16 GEMM: a pipeline wait timed out");
   }
   return QMCKL_SUCCESS_DEVICE;
+}
+
+// out[rows][M] = split-BF16 product of the A planes ap ([3][rows][kp]) and the coefficients.
+static qmckl_exit_code_device contract_planes(Ctx* ctx, qmckl_context_device c, const __nv_bfloat16* ap, int64_t rows,
+                                              int64_t kp, int* err, double* out, const char* name) {
+  MoBasisData& mo = ctx->mo_basis;
+  SplitJob job;
+  const int tiles =
+      make_job(job, ap, rows, static_cast<const __nv_bfloat16*>(mo.coef_split), mo.mo_num, kp, out, 0);
+  return run_job(ctx, c, job, tiles, err, name);
 }
 
 // Ensures the A-plane buffer holds rows x kp planes plus the error word; returns the error word.
@@ -610,7 +694,7 @@ static qmckl_exit_code_device split_mo_vgl(Ctx* ctx, qmckl_context_device c, dou
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
   const int64_t P = ctx->point.num, A = ctx->ao_basis.ao_num, M = ctx->mo_basis.mo_num;
   if (P <= 0 || M <= 0) return QMCKL_SUCCESS_DEVICE;
-  const int64_t rows = 5 * P, kp = round_up(A, kBK);
+  const int64_t pp = round_up(P, 32), rows = 5 * pp, kp = round_up(A, kBK);
   if (rows > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
   qmckl_exit_code_device rc = ensure_tables(ctx, c);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -619,8 +703,12 @@ static qmckl_exit_code_device split_mo_vgl(Ctx* ctx, qmckl_context_device c, dou
   int* err = ensure_a_planes(ctx, rows, kp);
   if (!err) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
   __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(ctx->mo_basis.ao_split);
-  launch_ao_planes(ctx, ctx->ao_basis.tables, ctx->point.coord, point_order(ctx), P, kp, ap);
-  return contract_planes(ctx, c, ap, rows, kp, err, out, "mo_vgl_split_bf16");
+  const int32_t* perm = point_order(ctx);
+  launch_ao_planes(ctx, ctx->ao_basis.tables, ctx->point.coord, perm, P, kp, ap);
+  SplitJob job;
+  const int tiles = make_job_mn(job, ap, pp, P, perm, static_cast<const __nv_bfloat16*>(ctx->mo_basis.coef_split),
+                                M, kp, out, 0);
+  return run_job(ctx, c, job, tiles, err, "mo_vgl_split_bf16");
 }
 
 size_t split_job_bytes() { return sizeof(SplitJob); }
@@ -629,6 +717,12 @@ int split_make_job(void* job_host, const void* a_planes, int64_t rows, const voi
                    double* out, int tile_begin, int n_cap) {
   return make_job(*static_cast<SplitJob*>(job_host), static_cast<const __nv_bfloat16*>(a_planes), rows,
                   static_cast<const __nv_bfloat16*>(b_planes), M, kp, out, tile_begin, n_cap);
+}
+
+int split_make_job_mn(void* job_host, const void* a_planes, int64_t pp, int64_t npts, const int32_t* perm,
+                      const void* b_planes, int64_t M, int64_t kp, double* out, int tile_begin, int n_cap) {
+  return make_job_mn(*static_cast<SplitJob*>(job_host), static_cast<const __nv_bfloat16*>(a_planes), pp, npts, perm,
+                     static_cast<const __nv_bfloat16*>(b_planes), M, kp, out, tile_begin, n_cap);
 }
 
 cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, int total_tiles, int* err) {
