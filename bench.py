@@ -46,7 +46,9 @@ def parse():
     p.add_argument("--electrons", type=int, default=160)
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--no-batched", action="store_true", help="skip the 64-molecule batched-form measurement")
+    p.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    p.add_argument("--batch-molecules", type=int, default=64, help="molecules of the batched workload")
+    p.add_argument("--batch-walkers", type=int, default=32, help="walkers per molecule of the batched workload")
     return p.parse_args()
 
 
@@ -153,16 +155,19 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the dominant kernels from the committed ncu summary
-    (profiles/ncu_traffic.txt, lines `kernel=<name> dram_bytes_per_point=<x>`)."""
-    out = {}
+    """Per-point DRAM bytes (and FP64-pipe activity, where measured) of the dominant kernels from
+    the committed ncu summary (profiles/ncu_traffic.txt, lines `kernel=<name>
+    dram_bytes_per_point=<x> [fp64_pipe_active=<f>]`)."""
+    out, pipe = {}, {}
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if os.path.exists(path):
         for line in open(path):
             if line.startswith("kernel="):
                 kv = dict(t.split("=", 1) for t in line.split())
                 out[kv["kernel"]] = float(kv["dram_bytes_per_point"])
-    return out
+                if "fp64_pipe_active" in kv:
+                    pipe[kv["kernel"]] = float(kv["fp64_pipe_active"])
+    return out, pipe
 
 
 def cpu_baseline(s, seconds, threads=None):
@@ -287,13 +292,13 @@ def time_e2e(ctx, s, steps, warmup):
     return dt, coord.nbytes, out.nbytes, out
 
 
-def time_batched(dist, steps, warmup, peaks, fp64_peak):
+def time_batched(dist, steps, warmup, peaks, fp64_peak, molecules=64, walkers=32):
     """The batched form on the 64-molecule workload: every member's MO vgl per step through
     qmckl_batch_provide_mo_vgl_device (graph replay, autotuned), both precision forms, plus
     one profiled pass with ordinary launches for the per-stage times."""
     from qmckl_sycl_gb300 import Batch, Context, config_batched
 
-    systems = config_batched(0)
+    systems = config_batched(0, molecules=molecules, walkers=walkers)
     ctxs = []
     for sy in systems:
         c = Context(dist.local_rank)
@@ -305,11 +310,11 @@ def time_batched(dist, steps, warmup, peaks, fp64_peak):
     ao_bytes = {"fp64": sum((8.0 * 5 * sy.ao_num + 24.0) * sy.point_num for sy in systems),
                 "mixed": sum((6.0 * 5 * sy.ao_num + 24.0) * sy.point_num for sy in systems)}
     flops = sum(10.0 * sy.ao_num * sy.mo_num * sy.point_num for sy in systems)
-    out = {"workload": "batched: %d molecules (%d-%d nuclei, %d-%d AOs, %d-%d MOs), 32 walkers x 2N electrons "
+    out = {"workload": "batched: %d molecules (%d-%d nuclei, %d-%d AOs, %d-%d MOs), %d walkers x 2N electrons "
                        "each, %d points in total" % (
                            len(systems), min(x.nucl_num for x in systems), max(x.nucl_num for x in systems),
                            min(x.ao_num for x in systems), max(x.ao_num for x in systems),
-                           min(x.mo_num for x in systems), max(x.mo_num for x in systems), P),
+                           min(x.mo_num for x in systems), max(x.mo_num for x in systems), walkers, P),
            "point_num": P, "forms": {}}
     ref = None
     for form, mode in (("fp64", 0), ("mixed", 1)):
@@ -447,7 +452,7 @@ def main():
     fp64_peak = ctypes.c_double(0)
     ctx.call("measure_fp64_peak", ctypes.byref(fp64_peak))
     peaks, peak_src = measured_peaks()
-    traffic = ncu_traffic()
+    traffic, fp64_pipe = ncu_traffic()
 
     forms = ["fp64"]
     try:
@@ -501,6 +506,9 @@ def main():
                 out[k] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                           "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
                 out[k]["frac"] = out[k]["achieved"] / peaks["hbm_gbs"]
+                if k in fp64_pipe:
+                    # what actually bounds it on GB300: FP64 issue (ncu, profiles/ao_vgl_fused_medium.md)
+                    out[k]["fp64_pipe_active_ncu"] = fp64_pipe[k]
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
             if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]
@@ -528,7 +536,8 @@ def main():
     adj = time_adjoint(dist, args.steps, args.warmup, fp64_peak.value)
     bt = None
     if not args.no_batched:
-        bt = time_batched(dist, args.steps, args.warmup, peaks, fp64_peak.value)
+        bt = time_batched(dist, args.steps, args.warmup, peaks, fp64_peak.value, args.batch_molecules,
+                          args.batch_walkers)
         bt["mixed_over_plain_fp64_medium"] = bt["forms"]["mixed"]["value"] / results["fp64"]["value"]
     if dist.rank != 0:
         return

@@ -181,16 +181,23 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// tcgen05.ld of 16 consecutive columns (32 lanes x 32 bit), not yet waited for.
+__device__ __forceinline__ void tmem_ld16_async(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
         "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+// Waits for every outstanding tcgen05.ld of the thread; r is passed through so that its uses
+// cannot be scheduled before the wait (call it for each array loaded; only the first waits).
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[16]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15])
+               :
+               : "memory");
 }
 
 // One contraction (one molecule): its six operand tensor maps and output. Jobs live in
@@ -407,24 +414,31 @@ __global__ void __launch_bounds__(kThreads, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // one TMEM round trip per 16 columns: the main block and the running (hi, lo) together
         for (int c0 = 0; c0 < N; c0 += 16) {
-          float v[16], hi[16], lo[16];
-          tmem_ld16(lb + (uint32_t)((1 + b) * N + c0), v);
+          uint32_t rv[16], rh[16], rl[16];
+          float hi[16], lo[16];
+          tmem_ld16_async(lb + (uint32_t)((1 + b) * N + c0), rv);
+          if (kb > 0) {
+            tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
+            tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
+          }
+          tmem_wait_ld(rv);
           if (kb == 0) {
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
-              hi[q] = v[q];
+              hi[q] = __uint_as_float(rv[q]);
               lo[q] = 0.f;
             }
           } else {
-            tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
-            tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
+            tmem_wait_ld(rh);
+            tmem_wait_ld(rl);
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               float s2, e2;
-              two_sum(hi[q], v[q], s2, e2);
+              two_sum(__uint_as_float(rh[q]), __uint_as_float(rv[q]), s2, e2);
               hi[q] = s2;
-              lo[q] += e2;
+              lo[q] = __uint_as_float(rl[q]) + e2;
             }
           }
           tmem_st16(lb + hi_col + (uint32_t)c0, hi);
@@ -437,23 +451,26 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (ok) {
         // the last accf phase covered every MMA of the tile, corrections included
+        int64_t orow = row < job.rows ? row : -1;
+        if (job.a_mn && orow >= 0) {
+          const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+          orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
+        }
         for (int c0 = 0; c0 < N; c0 += 16) {
-          float c[16], hi[16], lo[16];
-          tmem_ld16(lb + (uint32_t)c0, c);
-          tmem_ld16(lb + hi_col + (uint32_t)c0, hi);
-          tmem_ld16(lb + lo_col + (uint32_t)c0, lo);
-          int64_t orow = row < job.rows ? row : -1;
-          if (job.a_mn && orow >= 0) {
-            const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
-            orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
-          }
+          uint32_t rc[16], rh[16], rl[16];
+          tmem_ld16_async(lb + (uint32_t)c0, rc);
+          tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
+          tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
+          tmem_wait_ld(rc);
+          tmem_wait_ld(rh);
+          tmem_wait_ld(rl);
           if (orow >= 0) {
             double* o = job.out + orow * job.ldo + n0 + c0;
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               float s2, e2;
-              two_sum(hi[q], c[q], s2, e2);
-              if (n0 + c0 + q < job.cols) o[q] = f32_to_f64_int(s2) + f32_to_f64_int(lo[q] + e2);
+              two_sum(__uint_as_float(rh[q]), __uint_as_float(rc[q]), s2, e2);
+              if (n0 + c0 + q < job.cols) o[q] = f32_to_f64_int(s2) + f32_to_f64_int(__uint_as_float(rl[q]) + e2);
             }
           }
         }
