@@ -408,8 +408,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool ok = true;
       for (int kb = 0; kb < job.kblocks; ++kb) {
         const int b = kb & 1, use = kb >> 1;
-        if (!wait_or_abort(&accf[b], (uint32_t)use & 1u, abort_flag)) {
-          set_abort(abort_flag, error, 4);
+        // warp-uniform decision: the tcgen05.ld/st below are .sync.aligned
+        if (!__all_sync(0xffffffffu, wait_or_abort(&accf[b], (uint32_t)use & 1u, abort_flag))) {
+          if (lane == 0) set_abort(abort_flag, error, 4);
           ok = false;
           break;
         }
@@ -450,12 +451,17 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&acce[b]);
       }
       if (ok) {
-        // the last accf phase covered every MMA of the tile, corrections included
+        // The last accf phase covered every MMA of the tile, corrections included, so the stage
+        // buffers are free (the next tile's loads start after the barrier below): each epilogue
+        // warp stages its 32 rows there and writes them as contiguous row segments (one thread
+        // per row would write 32 scattered 8-byte pieces per instruction).
         int64_t orow = row < job.rows ? row : -1;
         if (job.a_mn && orow >= 0) {
           const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
           orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
         }
+        const int pitch = N + 1;  // doubles; odd pitch spreads the rows over the banks
+        double* stg = reinterpret_cast<double*>(base) + (size_t)quarter * 32 * pitch;
         for (int c0 = 0; c0 < N; c0 += 16) {
           uint32_t rc[16], rh[16], rl[16];
           tmem_ld16_async(lb + (uint32_t)c0, rc);
@@ -464,20 +470,37 @@ __global__ void __launch_bounds__(kThreads, 1)
           tmem_wait_ld(rc);
           tmem_wait_ld(rh);
           tmem_wait_ld(rl);
-          if (orow >= 0) {
-            double* o = job.out + orow * job.ldo + n0 + c0;
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              float s2, e2;
-              two_sum(__uint_as_float(rh[q]), __uint_as_float(rc[q]), s2, e2);
-              if (n0 + c0 + q < job.cols) o[q] = f32_to_f64_int(s2) + f32_to_f64_int(__uint_as_float(rl[q]) + e2);
-            }
+          for (int q = 0; q < 16; ++q) {
+            float s2, e2;
+            two_sum(__uint_as_float(rh[q]), __uint_as_float(rc[q]), s2, e2);
+            // hi + (lo + e) rounded once to FP32 (2^-24 relative) and widened exactly: an FP64 add
+            // here would cost the FP64 pipe ~10k cycles per tile
+            stg[lane * pitch + c0 + q] = f32_to_f64_int(s2 + (__uint_as_float(rl[q]) + e2));
           }
         }
+        __syncwarp();
+        const int ncol = (int)(job.cols - n0 < N ? job.cols - n0 : N);
+        // rows four at a time, so that the shared loads and global stores of a lane overlap
+        for (int r0 = 0; r0 < 32; r0 += 4) {
+          int64_t orr[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) orr[u] = __shfl_sync(0xffffffffu, orow, r0 + u);
+          for (int c = lane; c < ncol; c += 32) {
+            double v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = stg[(r0 + u) * pitch + c];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (orr[u] >= 0) job.out[orr[u] * job.ldo + n0 + c] = v[u];
+          }
+        }
+        // these generic-proxy accesses must be ordered before the next tile's TMA writes
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
     }
     // no MMA of this tile may still run when its barriers and tensor memory are reused
-    if (warp == 1 && lane == 0) mbar_wait(mma_done, 0);
+    if (warp == 1 && lane == 0 && !mbar_wait(mma_done, 0)) set_abort(abort_flag, error, 5);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
