@@ -261,23 +261,53 @@ __device__ __forceinline__ void set_abort(volatile int* abort_flag, int* error, 
   atomicExch(error, code);
 }
 
+// Output staging of the epilogue: 4 warps x 32 rows x (kMaxN + 1) FP32 values.
+constexpr uint32_t kOutStage = 4 * 32 * (kMaxN + 1) * 4;
+
+// Tile geometry of launch tile `tile`: its job and the job-local row / column origins.
+struct TileRef {
+  const SplitJob* job;
+  int m0, n0;
+};
+__device__ __forceinline__ TileRef tile_ref(const SplitJob* __restrict__ jobs, int njobs, int tile) {
+  int j = 0, hi = njobs - 1;  // last job whose first tile is <= tile
+  while (j < hi) {
+    const int mid = (j + hi + 1) >> 1;
+    if (jobs[mid].tile_begin <= tile) j = mid;
+    else hi = mid - 1;
+  }
+  const SplitJob* job = &jobs[j];
+  const int local = tile - job->tile_begin;
+  TileRef t;
+  t.job = job;
+  t.m0 = (local / job->col_tiles) * kBM;
+  t.n0 = (local % job->col_tiles) * job->n_tile;
+  return t;
+}
+
 // Tensor-memory columns: [0,N) corrections, [N,2N) and [2N,3N) main product ping-pong
 // buffers (one 64-wide K block each), [3N,4N) and [4N,5N) the running FP32 two-sum (hi, lo)
 // of the main product, folded in by the epilogue warps after every K block.
 //
-// Persistent: CTA b processes tiles b, b + gridDim.x, ... of the launch (tiles of one job
-// are ordered column tile fastest, so CTAs running at the same time share A rows in L2).
-// Tensor memory (512 columns) is allocated once; the barriers are re-initialised per tile.
+// Persistent and continuous: CTA b processes tiles b, b + gridDim.x, ... of the launch (tiles
+// of one job are ordered column tile fastest, so CTAs running at the same time share A rows in
+// L2). The three roles walk the same sequence of (tile, K block) steps with running barrier
+// phases, so the producer prefetches the next tile while the epilogue finishes the current one;
+// the only hand-over between tiles is `tmem_free`: the MMA issuer starts a tile once the
+// epilogue has read the previous tile's accumulators out of tensor memory (the epilogue then
+// writes that tile's output from its own staging buffer while the next tile computes).
 __global__ void __launch_bounds__(kThreads, 1)
     split_gemm_kernel(const SplitJob* __restrict__ jobs, int njobs, int total_tiles, int* error) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t max_stage = 3 * kPlaneA + 3 * (uint32_t)kMaxN * kBK * 2;
-  uint64_t* full = (uint64_t*)(base + kStages * max_stage);
+  float* out_stage = (float*)(base + kStages * max_stage);
+  uint64_t* full = (uint64_t*)(base + kStages * max_stage + kOutStage);
   uint64_t* empty = full + kStages;
   uint64_t* accf = empty + kStages;  // [2] main buffer filled (MMA -> epilogue)
   uint64_t* acce = accf + 2;         // [2] main buffer folded (epilogue -> MMA)
-  uint64_t* mma_done = acce + 2;
+  uint64_t* tmem_free = acce + 2;    // accumulators of the last tile read out (epilogue -> MMA)
+  uint64_t* mma_done = tmem_free + 1;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
   const uint32_t tmem_cols = 512;
@@ -288,99 +318,97 @@ __global__ void __launch_bounds__(kThreads, 1)
                  "r"(tmem_cols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
-  if (threadIdx.x == 0) *abort_flag = 0;
+  if (threadIdx.x == 0) {
+    *abort_flag = 0;
+    for (int s2 = 0; s2 < kStages; ++s2) {
+      mbar_init(&full[s2], 1);
+      mbar_init(&empty[s2], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], 4);
+    }
+    mbar_init(tmem_free, 4);
+    mbar_init(mma_done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  int done_phases = 0;  // mma_done completions so far (one per tile with MMAs issued)
-  for (int tile = blockIdx.x; tile < total_tiles && !*abort_flag; tile += gridDim.x) {
-    int j = 0, hi = njobs - 1;  // last job whose first tile is <= tile
-    while (j < hi) {
-      const int mid = (j + hi + 1) >> 1;
-      if (jobs[mid].tile_begin <= tile) j = mid;
-      else hi = mid - 1;
-    }
-    const SplitJob& job = jobs[j];
-    const int local = tile - job.tile_begin;
-    const int N = job.n_tile;
-    const int m0 = (local / job.col_tiles) * kBM;
-    const int n0 = (local % job.col_tiles) * N;
-    const uint32_t plane_b = (uint32_t)N * kBK * 2;
-    const uint32_t stage_bytes = 3 * kPlaneA + 3 * plane_b;
-
-    if (threadIdx.x == 0) {
-      for (int s2 = 0; s2 < kStages; ++s2) {
-        mbar_init(&full[s2], 1);
-        mbar_init(&empty[s2], 1);
-      }
-      for (int b = 0; b < 2; ++b) {
-        mbar_init(&accf[b], 1);
-        mbar_init(&acce[b], 4);
-      }
-      mbar_init(mma_done, 1);
-      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
-    if (warp == 0) {
-      if (lane == 0) {
-        for (int i = 0; i < 3; ++i) {
-          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((uint64_t)&job.ta[i]) : "memory");
-          asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"((uint64_t)&job.tb[i]) : "memory");
-        }
-        int issued = 0;
-        bool ok = true;
-        for (int kb = 0; kb < job.kblocks; ++kb) {
-          const int s2 = kb % kStages;
-          const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---------------- TMA producer
+      uint32_t it = 0;  // running K-block index over the CTA's tiles
+      bool ok = true;
+      for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
+        const TileRef tr = tile_ref(jobs, njobs, tile);
+        const SplitJob& job = *tr.job;
+        const uint32_t plane_b = (uint32_t)job.n_tile * kBK * 2;
+        const uint32_t stage_bytes = 3 * kPlaneA + 3 * plane_b;
+        for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
+          const uint32_t s2 = it % kStages, ph = (it / kStages) & 1u;
           if (!wait_or_abort(&empty[s2], ph ^ 1u, abort_flag)) {
-            ok = false;
             set_abort(abort_flag, error, 1);
+            ok = false;
             break;
           }
-          unsigned char* st = base + s2 * stage_bytes;
+          unsigned char* st = base + s2 * max_stage;
           mbar_expect_tx(&full[s2], stage_bytes);
           if (job.a_mn) {
             // two 64(M) x 64(K) boxes per plane: M rows m0..m0+63, then m0+64..m0+127
             for (int i = 0; i < 3; ++i) {
-              tma_load_2d(st + i * kPlaneA, &job.ta[i], m0, kb * kBK, &full[s2]);
-              tma_load_2d(st + i * kPlaneA + kPlaneA / 2, &job.ta[i], m0 + 64, kb * kBK, &full[s2]);
+              tma_load_2d(st + i * kPlaneA, &job.ta[i], tr.m0, kb * kBK, &full[s2]);
+              tma_load_2d(st + i * kPlaneA + kPlaneA / 2, &job.ta[i], tr.m0 + 64, kb * kBK, &full[s2]);
             }
           } else {
-            for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, &job.ta[i], kb * kBK, m0, &full[s2]);
+            for (int i = 0; i < 3; ++i) tma_load_2d(st + i * kPlaneA, &job.ta[i], kb * kBK, tr.m0, &full[s2]);
           }
-          for (int i = 0; i < 3; ++i) tma_load_2d(st + 3 * kPlaneA + i * plane_b, &job.tb[i], kb * kBK, n0, &full[s2]);
-          issued = kb + 1;
-        }
-        if (!ok) {
-          // drain the loads still in flight before the shared memory is reused or released
-          for (int kb = issued - kStages < 0 ? 0 : issued - kStages; kb < issued; ++kb)
-            mbar_wait(&full[kb % kStages], (uint32_t)(kb / kStages) & 1u);
+          for (int i = 0; i < 3; ++i)
+            tma_load_2d(st + 3 * kPlaneA + i * plane_b, &job.tb[i], kb * kBK, tr.n0, &full[s2]);
         }
       }
-    } else if (warp == 1) {
-      if (lane == 0) {
+      // the loads still in flight must land before the shared memory is released
+      const uint32_t first = it > (uint32_t)kStages ? it - kStages : 0;
+      for (uint32_t q = first; q < it; ++q) mbar_wait(&full[q % kStages], (q / kStages) & 1u);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---------------- MMA issuer
+      uint32_t it = 0, tl = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x, ++tl) {
+        const TileRef tr = tile_ref(jobs, njobs, tile);
+        const SplitJob& job = *tr.job;
+        const int N = job.n_tile;
+        const uint32_t plane_b = (uint32_t)N * kBK * 2;
         // D = F32 (bit 4), A = B = BF16 (bits 7, 10), A M-major (bit 15) when a_mn, N >> 3, M >> 4
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((job.a_mn ? 1u : 0u) << 15) |
                                ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
         const bool amn = job.a_mn != 0;
-        for (int kb = 0; kb < job.kblocks; ++kb) {
-          const int s2 = kb % kStages, b = kb & 1, use = kb >> 1;
-          const uint32_t ph = (uint32_t)(kb / kStages) & 1u;
-          if (use > 0 && !wait_or_abort(&acce[b], (uint32_t)(use - 1) & 1u, abort_flag)) {
+        // the correction accumulator and the previous tile's two-sum are read out before reuse
+        if (tl > 0 && !wait_or_abort(tmem_free, (tl - 1) & 1u, abort_flag)) {
+          set_abort(abort_flag, error, 6);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
+          const uint32_t s2 = it % kStages, ph = (it / kStages) & 1u, b = it & 1u, use = it >> 1;
+          if (use > 0 && !wait_or_abort(&acce[b], (use - 1) & 1u, abort_flag)) {
             set_abort(abort_flag, error, 2);
+            ok = false;
             break;
           }
           if (!wait_or_abort(&full[s2], ph, abort_flag)) {
             set_abort(abort_flag, error, 3);
+            ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t sa = smem_u32(base + s2 * stage_bytes);
+          const uint32_t sa = smem_u32(base + s2 * max_stage);
           const uint32_t sb = sa + 3 * kPlaneA;
-          const uint32_t main_acc = tmem + (uint32_t)((1 + b) * N);
+          const uint32_t main_acc = tmem + (1 + b) * (uint32_t)N;
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
             // a K step of 16: 32 bytes along a K-major row, or 16 rows of 128 bytes (M-major)
@@ -397,19 +425,26 @@ __global__ void __launch_bounds__(kThreads, 1)
           umma_commit(&empty[s2]);  // frees the stage once these MMAs have read it
           umma_commit(&accf[b]);    // main buffer b holds this block's product
         }
-        umma_commit(mma_done);  // every MMA of this tile has completed
       }
-    } else {
-      // epilogue: warp w owns TMEM lanes 32*(w % 4) .. +31 (one output row per thread)
-      const int quarter = warp & 3;
-      const int64_t row = (int64_t)m0 + quarter * 32 + lane;
-      const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
+      umma_commit(mma_done);  // every MMA issued has completed
+      if (!mbar_wait(mma_done, 0)) set_abort(abort_flag, error, 5);
+    }
+  } else {
+    // ---------------- epilogue: warp w owns TMEM lanes 32*(w % 4) .. +31 (one row per thread)
+    const int quarter = warp & 3;
+    const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
+    float* stg = out_stage + (size_t)quarter * 32 * (kMaxN + 1);
+    uint32_t it = 0, tl = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x, ++tl) {
+      const TileRef tr = tile_ref(jobs, njobs, tile);
+      const SplitJob& job = *tr.job;
+      const int N = job.n_tile;
       const uint32_t hi_col = 3 * N, lo_col = 4 * N;
-      bool ok = true;
-      for (int kb = 0; kb < job.kblocks; ++kb) {
-        const int b = kb & 1, use = kb >> 1;
+      for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
+        const uint32_t b = it & 1u, use = it >> 1;
         // warp-uniform decision: the tcgen05.ld/st below are .sync.aligned
-        if (!__all_sync(0xffffffffu, wait_or_abort(&accf[b], (uint32_t)use & 1u, abort_flag))) {
+        if (!__all_sync(0xffffffffu, wait_or_abort(&accf[b], use & 1u, abort_flag))) {
           if (lane == 0) set_abort(abort_flag, error, 4);
           ok = false;
           break;
@@ -419,7 +454,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int c0 = 0; c0 < N; c0 += 16) {
           uint32_t rv[16], rh[16], rl[16];
           float hi[16], lo[16];
-          tmem_ld16_async(lb + (uint32_t)((1 + b) * N + c0), rv);
+          tmem_ld16_async(lb + (1 + b) * (uint32_t)N + (uint32_t)c0, rv);
           if (kb > 0) {
             tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
             tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
@@ -450,63 +485,57 @@ __global__ void __launch_bounds__(kThreads, 1)
         __syncwarp();
         if (lane == 0) mbar_arrive(&acce[b]);
       }
-      if (ok) {
-        // The last accf phase covered every MMA of the tile, corrections included, so the stage
-        // buffers are free (the next tile's loads start after the barrier below): each epilogue
-        // warp stages its 32 rows there and writes them as contiguous row segments (one thread
-        // per row would write 32 scattered 8-byte pieces per instruction).
-        int64_t orow = row < job.rows ? row : -1;
-        if (job.a_mn && orow >= 0) {
-          const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
-          orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
-        }
-        const int pitch = N + 1;  // doubles; odd pitch spreads the rows over the banks
-        double* stg = reinterpret_cast<double*>(base) + (size_t)quarter * 32 * pitch;
-        for (int c0 = 0; c0 < N; c0 += 16) {
-          uint32_t rc[16], rh[16], rl[16];
-          tmem_ld16_async(lb + (uint32_t)c0, rc);
-          tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
-          tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
-          tmem_wait_ld(rc);
-          tmem_wait_ld(rh);
-          tmem_wait_ld(rl);
-#pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            float s2, e2;
-            two_sum(__uint_as_float(rh[q]), __uint_as_float(rc[q]), s2, e2);
-            // hi + (lo + e) rounded once to FP32 (2^-24 relative) and widened exactly: an FP64 add
-            // here would cost the FP64 pipe ~10k cycles per tile
-            stg[lane * pitch + c0 + q] = f32_to_f64_int(s2 + (__uint_as_float(rl[q]) + e2));
-          }
-        }
-        __syncwarp();
-        const int ncol = (int)(job.cols - n0 < N ? job.cols - n0 : N);
-        // rows four at a time, so that the shared loads and global stores of a lane overlap
-        for (int r0 = 0; r0 < 32; r0 += 4) {
-          int64_t orr[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) orr[u] = __shfl_sync(0xffffffffu, orow, r0 + u);
-          for (int c = lane; c < ncol; c += 32) {
-            double v[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = stg[(r0 + u) * pitch + c];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-              if (orr[u] >= 0) job.out[orr[u] * job.ldo + n0 + c] = v[u];
-          }
-        }
-        // these generic-proxy accesses must be ordered before the next tile's TMA writes
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (!ok) break;
+      // The last accf phase covered every MMA of the tile, corrections included: read the
+      // accumulators out into the staging buffer, release tensor memory to the next tile, then
+      // write the rows as contiguous segments (one thread per row would write 32 scattered
+      // 8-byte pieces per instruction).
+      const int64_t row = (int64_t)tr.m0 + quarter * 32 + lane;
+      int64_t orow = row < job.rows ? row : -1;
+      if (job.a_mn && orow >= 0) {
+        const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+        orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
       }
+      const int pitch = kMaxN + 1;  // odd pitch spreads the rows over the banks
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        uint32_t rc[16], rh[16], rl[16];
+        tmem_ld16_async(lb + (uint32_t)c0, rc);
+        tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
+        tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
+        tmem_wait_ld(rc);
+        tmem_wait_ld(rh);
+        tmem_wait_ld(rl);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          float s2, e2;
+          two_sum(__uint_as_float(rh[q]), __uint_as_float(rc[q]), s2, e2);
+          // hi + (lo + e) rounded once to FP32 (2^-24 relative); an FP64 add here would cost the
+          // FP64 pipe ~10k cycles per tile
+          stg[lane * pitch + c0 + q] = s2 + (__uint_as_float(rl[q]) + e2);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tmem_free);
+      const int ncol = (int)(job.cols - tr.n0 < N ? job.cols - tr.n0 : N);
+      // rows four at a time, so that the shared loads and global stores of a lane overlap
+      for (int r0 = 0; r0 < 32; r0 += 4) {
+        int64_t orr[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) orr[u] = __shfl_sync(0xffffffffu, orow, r0 + u);
+        for (int c = lane; c < ncol; c += 32) {
+          double v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = f32_to_f64_int(stg[(r0 + u) * pitch + c]);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            if (orr[u] >= 0) job.out[orr[u] * job.ldo + tr.n0 + c] = v[u];
+        }
+      }
+      __syncwarp();  // the staging buffer is rewritten by the next tile
     }
-    // no MMA of this tile may still run when its barriers and tensor memory are reused
-    if (warp == 1 && lane == 0 && !mbar_wait(mma_done, 0)) set_abort(abort_flag, error, 5);
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    ++done_phases;
   }
-  (void)done_phases;
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -621,7 +650,9 @@ int make_job_mn(SplitJob& job, const __nv_bfloat16* ap, int64_t pp, int64_t npts
   return (int)((rows + kBM - 1) / kBM) * job.col_tiles;
 }
 
-size_t split_smem_bytes() { return 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)kMaxN * kBK * 2) + 256; }
+size_t split_smem_bytes() {
+  return 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)kMaxN * kBK * 2) + kOutStage + 256;
+}
 
 // One persistent launch over every tile of the njobs jobs at d_jobs (device memory).
 cudaError_t launch_split_jobs(cudaStream_t stream, const SplitJob* d_jobs, int njobs, int total_tiles, int* err) {
