@@ -45,7 +45,7 @@ constexpr int kBM = 128;        // rows per tile (UMMA M)
 constexpr int kBK = 64;         // K per stage: 64 BF16 = 128 bytes = one swizzle row
 constexpr int kStages = 2;
 constexpr int kMaxN = 96;       // columns per tile: 5 * N <= 512 TMEM columns
-constexpr int kThreads = 192;   // 6 warps
+constexpr int kThreads = 320;   // 10 warps: TMA, MMA, 4 fold warps, 4 store warps
 constexpr uint32_t kPlaneA = kBM * kBK * 2;  // 16 KB per A plane and stage
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
 
@@ -307,7 +307,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   uint64_t* accf = empty + kStages;  // [2] main buffer filled (MMA -> epilogue)
   uint64_t* acce = accf + 2;         // [2] main buffer folded (epilogue -> MMA)
   uint64_t* tmem_free = acce + 2;    // accumulators of the last tile read out (epilogue -> MMA)
-  uint64_t* mma_done = tmem_free + 1;
+  uint64_t* out_ready = tmem_free + 1;  // staging buffer filled (fold warps -> store warps)
+  uint64_t* out_free = out_ready + 1;   // staging buffer written out (store warps -> fold warps)
+  uint64_t* mma_done = out_free + 1;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
   const uint32_t tmem_cols = 512;
@@ -329,6 +331,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&acce[b], 4);
     }
     mbar_init(tmem_free, 4);
+    mbar_init(out_ready, 4);
+    mbar_init(out_free, 4);
     mbar_init(mma_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -429,8 +433,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       umma_commit(mma_done);  // every MMA issued has completed
       if (!mbar_wait(mma_done, 0)) set_abort(abort_flag, error, 5);
     }
-  } else {
-    // ---------------- epilogue: warp w owns TMEM lanes 32*(w % 4) .. +31 (one row per thread)
+  } else if (warp < 6) {
+    // ---------------- fold warps: warp w owns TMEM lanes 32*(w % 4) .. +31 (one row per thread)
     const int quarter = warp & 3;
     const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
     float* stg = out_stage + (size_t)quarter * 32 * (kMaxN + 1);
@@ -487,14 +491,12 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       if (!ok) break;
       // The last accf phase covered every MMA of the tile, corrections included: read the
-      // accumulators out into the staging buffer, release tensor memory to the next tile, then
-      // write the rows as contiguous segments (one thread per row would write 32 scattered
-      // 8-byte pieces per instruction).
-      const int64_t row = (int64_t)tr.m0 + quarter * 32 + lane;
-      int64_t orow = row < job.rows ? row : -1;
-      if (job.a_mn && orow >= 0) {
-        const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
-        orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
+      // accumulators out into the staging buffer (once the store warps have written out the
+      // previous tile), then release tensor memory to the next tile and the staging buffer to the
+      // store warps.
+      if (tl > 0 && !__all_sync(0xffffffffu, wait_or_abort(out_free, (tl - 1) & 1u, abort_flag))) {
+        if (lane == 0) set_abort(abort_flag, error, 7);
+        break;
       }
       const int pitch = kMaxN + 1;  // odd pitch spreads the rows over the banks
       for (int c0 = 0; c0 < N; c0 += 16) {
@@ -516,8 +518,29 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
-      if (lane == 0) mbar_arrive(tmem_free);
-      const int ncol = (int)(job.cols - tr.n0 < N ? job.cols - tr.n0 : N);
+      if (lane == 0) {
+        mbar_arrive(tmem_free);
+        mbar_arrive(out_ready);
+      }
+    }
+  } else {
+    // ---------------- store warps: write each tile's staged rows as contiguous row segments
+    // (one thread per row would write 32 scattered 8-byte pieces per instruction)
+    const int quarter = warp & 3;
+    const float* stg = out_stage + (size_t)quarter * 32 * (kMaxN + 1);
+    const int pitch = kMaxN + 1;
+    uint32_t tl = 0;
+    for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x, ++tl) {
+      const TileRef tr = tile_ref(jobs, njobs, tile);
+      const SplitJob& job = *tr.job;
+      const int64_t row = (int64_t)tr.m0 + quarter * 32 + lane;
+      int64_t orow = row < job.rows ? row : -1;
+      if (job.a_mn && orow >= 0) {
+        const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+        orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
+      }
+      if (!__all_sync(0xffffffffu, wait_or_abort(out_ready, tl & 1u, abort_flag))) break;
+      const int ncol = (int)(job.cols - tr.n0 < job.n_tile ? job.cols - tr.n0 : job.n_tile);
       // rows four at a time, so that the shared loads and global stores of a lane overlap
       for (int r0 = 0; r0 < 32; r0 += 4) {
         int64_t orr[4];
@@ -532,7 +555,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (orr[u] >= 0) job.out[orr[u] * job.ldo + tr.n0 + c] = v[u];
         }
       }
-      __syncwarp();  // the staging buffer is rewritten by the next tile
+      __syncwarp();
+      if (lane == 0) mbar_arrive(out_free);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
