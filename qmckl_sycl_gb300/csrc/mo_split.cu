@@ -176,6 +176,25 @@ __device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t 
           tmem_d),
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
+// The six MMAs of one K step, issued together: hi.hi into the main buffer d0 (accumulate flag
+// am), then hi.mid, mid.hi, hi.lo, mid.mid, lo.hi into the correction accumulator d1 (flag ac for
+// the first, accumulate for the rest). Descriptors come precomputed: the issuing thread's
+// instruction count per MMA sets its issue rate.
+__device__ __forceinline__ void umma_six(uint32_t d0, uint32_t d1, uint64_t a0, uint64_t b0, uint64_t a1, uint64_t b1,
+                                         uint64_t a2, uint64_t b2, uint64_t a3, uint64_t b3, uint64_t a4, uint64_t b4,
+                                         uint64_t a5, uint64_t b5, uint32_t idesc, uint32_t am, uint32_t ac) {
+  asm volatile(
+      "{\n .reg .pred pm, pc, pt;\n setp.ne.b32 pm, %15, 0;\n setp.ne.b32 pc, %16, 0;\n setp.eq.b32 pt, 0, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %2, %3, %14, pm;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%1], %4, %5, %14, pc;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%1], %6, %7, %14, pt;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%1], %8, %9, %14, pt;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%1], %10, %11, %14, pt;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%1], %12, %13, %14, pt;\n}\n" ::"r"(d0),
+      "r"(d1), "l"(a0), "l"(b0), "l"(a1), "l"(b1), "l"(a2), "l"(b2), "l"(a3), "l"(b3), "l"(a4), "l"(b4), "l"(a5),
+      "l"(b5), "r"(idesc), "r"(am), "r"(ac));
+}
+
 __device__ __forceinline__ void umma_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -222,9 +241,6 @@ struct alignas(64) SplitJob {
   const int32_t* perm;  // processing order (null: identity)
 };
 
-// Correction terms (A plane, B plane): hi*mid, mid*hi, hi*lo, mid*mid, lo*hi.
-__constant__ int kPairA[5] = {0, 1, 0, 1, 2};
-__constant__ int kPairB[5] = {1, 0, 2, 1, 0};
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
@@ -391,6 +407,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((job.a_mn ? 1u : 0u) << 15) |
                                ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
         const bool amn = job.a_mn != 0;
+        const uint64_t ka = amn ? 128u : 2u, pa = kPlaneA >> 4, pb = plane_b >> 4;
         // the correction accumulator and the previous tile's two-sum are read out before reuse
         if (tl > 0 && !wait_or_abort(tmem_free, (tl - 1) & 1u, abort_flag)) {
           set_abort(abort_flag, error, 6);
@@ -410,21 +427,18 @@ __global__ void __launch_bounds__(kThreads, 1)
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          // descriptors in 16-byte units: a K step is 2 (32 bytes along a K-major row) or 128
+          // (16 rows of 128 bytes, M-major); planes are kPlaneA / plane_b bytes apart
           const uint32_t sa = smem_u32(base + s2 * max_stage);
-          const uint32_t sb = sa + 3 * kPlaneA;
+          const uint64_t da = amn ? sdesc_mn(sa) : sdesc(sa);
+          const uint64_t db = sdesc(sa + 3 * kPlaneA);
           const uint32_t main_acc = tmem + (1 + b) * (uint32_t)N;
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
-            // a K step of 16: 32 bytes along a K-major row, or 16 rows of 128 bytes (M-major)
-            const uint64_t a0 = amn ? sdesc_mn(sa + kk * 2048) : sdesc(sa + kk * 32);
-            umma_bf16(main_acc, a0, sdesc(sb + kk * 32), idesc, kk > 0 ? 1u : 0u);
-#pragma unroll
-            for (int t = 0; t < 5; ++t) {
-              const uint32_t aa = sa + kPairA[t] * kPlaneA;
-              const uint64_t ad = amn ? sdesc_mn(aa + kk * 2048) : sdesc(aa + kk * 32);
-              const uint64_t bd = sdesc(sb + kPairB[t] * plane_b + kk * 32);
-              umma_bf16(tmem, ad, bd, idesc, (kb | kk | t) != 0);
-            }
+            const uint64_t a = da + kk * ka, bb = db + kk * 2u;
+            // (A plane, B plane): main (0,0); corrections (0,1) (1,0) (0,2) (1,1) (2,0)
+            umma_six(main_acc, tmem, a, bb, a, bb + pb, a + pa, bb, a, bb + 2 * pb, a + pa, bb + pb, a + 2 * pa, bb, idesc,
+                     kk > 0 ? 1u : 0u, (kb | kk) != 0 ? 1u : 0u);
           }
           umma_commit(&empty[s2]);  // frees the stage once these MMAs have read it
           umma_commit(&accf[b]);    // main buffer b holds this block's product
