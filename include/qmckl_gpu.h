@@ -47,6 +47,16 @@ typedef int64_t qmckl_context_device;
 #define QMCKL_INVALID_ARG_8_DEVICE ((qmckl_exit_code_device)8)
 #define QMCKL_INVALID_ARG_9_DEVICE ((qmckl_exit_code_device)9)
 #define QMCKL_INVALID_ARG_10_DEVICE ((qmckl_exit_code_device)10)
+#define QMCKL_INVALID_ARG_11_DEVICE ((qmckl_exit_code_device)11)
+#define QMCKL_INVALID_ARG_12_DEVICE ((qmckl_exit_code_device)12)
+#define QMCKL_INVALID_ARG_13_DEVICE ((qmckl_exit_code_device)13)
+#define QMCKL_INVALID_ARG_14_DEVICE ((qmckl_exit_code_device)14)
+#define QMCKL_INVALID_ARG_15_DEVICE ((qmckl_exit_code_device)15)
+#define QMCKL_INVALID_ARG_16_DEVICE ((qmckl_exit_code_device)16)
+#define QMCKL_INVALID_ARG_17_DEVICE ((qmckl_exit_code_device)17)
+#define QMCKL_INVALID_ARG_18_DEVICE ((qmckl_exit_code_device)18)
+#define QMCKL_INVALID_ARG_19_DEVICE ((qmckl_exit_code_device)19)
+#define QMCKL_INVALID_ARG_20_DEVICE ((qmckl_exit_code_device)20)
 #define QMCKL_FAILURE_DEVICE ((qmckl_exit_code_device)101)
 #define QMCKL_ERRNO_DEVICE ((qmckl_exit_code_device)102)
 #define QMCKL_INVALID_CONTEXT_DEVICE ((qmckl_exit_code_device)103)
@@ -357,6 +367,38 @@ qmckl_exit_code_device qmckl_exp_check_device(qmckl_context_device context, cons
 qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(const double* ao, int64_t rows, int64_t ao_num,
                                                                    const double* coefficient, int64_t mo_num,
                                                                    int32_t vgl_mask, double* out, void* cuda_stream);
+
+/* ---- Electron-nucleus and electron-electron distances ---------------------------------------
+ * src/qmckl_electron.cpp:192-552 of the reference (include/qmckl_electron.hpp:30-41,
+ * include/qmckl_gpu.hpp:1043-1046). C[i + j*ldc] = |A_i - B_j| for i < m, j < n, where point i of A
+ * is (A[0 + i*lda], A[1 + i*lda], A[2 + i*lda]) for transa 'N' and (A[i], A[i + lda], A[i + 2*lda])
+ * for 'T' (same for B with ldb); device pointers. The reference's kernel takes square roots of whole
+ * columns from every work-item (src/qmckl_electron.cpp:504-546); this one computes each entry once:
+ * sqrt((x*x + y*y) + z*z) rounded like the reference's host arithmetic. Argument checks as the
+ * reference's (bad trans: ARG_1; m, n <= 0: ARG_4/5; lda, ldb, ldc too small: ARG_7/9/11), with lda
+ * checked against transa and ldb against transb. */
+qmckl_exit_code_device qmckl_distance_device(const qmckl_context_device context, const char transa, const char transb,
+                                             const int64_t m, const int64_t n, const double* A, const int64_t lda,
+                                             const double* B, const int64_t ldb, double* const C, const int64_t ldc);
+/* en_distance[point][nucl] from coord [3][point_num] and nucl_coord [3][nucl_num]. */
+qmckl_exit_code_device qmckl_compute_en_distance_device(const qmckl_context_device context, const int64_t point_num,
+                                                        const int64_t nucl_num, const double* elec_coord,
+                                                        const double* nucl_coord, double* const en_distance);
+/* ee_distance[walker][j][i] for the elec_num electrons of each of the walk_num walkers; coord is the
+ * points array [3][walk_num * elec_num]. */
+qmckl_exit_code_device qmckl_compute_ee_distance_device(const qmckl_context_device context, const int64_t elec_num,
+                                                        const int64_t walk_num, const double* coord,
+                                                        double* const ee_distance);
+/* Date-cached providers (recomputed when the points changed). */
+qmckl_exit_code_device qmckl_provide_en_distance_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_provide_ee_distance_device(qmckl_context_device context);
+/* Getters (no counterpart in the reference, whose cached arrays are read only by its Jastrow code):
+ * copy the cached en_distance [point_num][nucl_num] / ee_distance [walk_num][elec_num][elec_num] to
+ * `distance` (device or host); size_max too small gives QMCKL_INVALID_ARG_3_DEVICE. */
+qmckl_exit_code_device qmckl_get_electron_en_distance_device(qmckl_context_device context, double* distance,
+                                                             int64_t size_max);
+qmckl_exit_code_device qmckl_get_electron_ee_distance_device(qmckl_context_device context, double* distance,
+                                                             int64_t size_max);
 
 /* ---- Batched form: many molecules of uneven size evaluated together ----------------------
  *

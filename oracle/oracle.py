@@ -65,6 +65,7 @@ def lib():
         L.oracle_shell_vgl.argtypes = [_I, _I, _I, _i64, _i64, _f64, _i64, _i64, _f64, _f64, _f64, _f64, _f64]
         L.oracle_mo_vgl.argtypes = [_I, _I, _I, _f64, _f64, _f64]
         L.oracle_mo_value.argtypes = [_I, _I, _I, _f64, _f64, _f64]
+        L.oracle_distance.argtypes = [ctypes.c_char, ctypes.c_char, _I, _I, _f64, _I, _f64, _I, _f64, _I]
         L.oracle_vjp_mo_vgl.restype = ctypes.c_int
         L.oracle_vjp_mo_vgl.argtypes = [_I, _f64, _I, _I, _I, _i64, _i64, _i32, _i64, _i64, _f64, _f64, _f64, _f64,
                                         _f64, _I, _f64, _I, _f64, _f64, _vp, _vp, _vp]
@@ -144,6 +145,34 @@ def vjp_mo_vgl(s, w, want=("coef", "expo", "coord"), coord_soa=None, threads=0):
                              np.ascontiguousarray(w, dtype=np.float64), _ptr(out.get("coef")), _ptr(out.get("expo")),
                              _ptr(out.get("coord")))
     assert rc == 0
+    return out
+
+
+def en_distance(s, coord_soa=None):
+    """en_distance[point][nucleus] (the reference's call: distance('T', 'T', N, P, nucl_coord, N,
+    coord, P, C, N))."""
+    L = lib()
+    if coord_soa is None:
+        coord_soa = np.ascontiguousarray(s.coord.T)
+    P = coord_soa.shape[1]
+    out = np.zeros((P, s.nucl_num))
+    L.oracle_distance(b"T", b"T", s.nucl_num, P, np.ascontiguousarray(s.nucl_coord), s.nucl_num,
+                      np.ascontiguousarray(coord_soa), P, out, s.nucl_num)
+    return out
+
+
+def ee_distance(coord_soa, elec_num, walk_num):
+    """ee_distance[walker][j][i] from the points [3][walk_num * elec_num]."""
+    L = lib()
+    out = np.zeros((walk_num, elec_num, elec_num))
+    ld = elec_num * walk_num
+    c = np.ascontiguousarray(coord_soa)
+    for k in range(walk_num):
+        sub = np.ascontiguousarray(c[:, k * elec_num:(k + 1) * elec_num])
+        blk = np.zeros((elec_num, elec_num))
+        L.oracle_distance(b"T", b"T", elec_num, elec_num, sub, elec_num, sub, elec_num, blk, elec_num)
+        out[k] = blk
+    del ld
     return out
 
 

@@ -644,3 +644,24 @@ int oracle_vjp_mo_vgl(int64_t nucl_num, const double* nucl_coord, int64_t shell_
   return 0;
 }
 #undef OR_D
+
+/* ======================================================================================
+ * Distances: the intended result of src/qmckl_electron.cpp:373-552 (qmckl_distance_device), which
+ * the reference's kernel garbles (every work-item takes square roots of a whole column of C):
+ * C[i + j*ldc] = sqrt((x*x + y*y) + z*z), x = A_i - B_j per coordinate, point i of A stored as
+ * A[d + i*lda] ('N') or A[i + d*lda] ('T'), same for B.
+ * ====================================================================================== */
+void oracle_distance(char transa, char transb, int64_t m, int64_t n, const double* A, int64_t lda, const double* B,
+                     int64_t ldb, double* C, int64_t ldc) {
+  const int ta = transa == 'T' || transa == 't', tb = transb == 'T' || transb == 't';
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < m; ++i) {
+      double d[3];
+      for (int k = 0; k < 3; ++k) {
+        const double a = ta ? A[i + k * lda] : A[k + i * lda];
+        const double b = tb ? B[j + k * ldb] : B[k + j * ldb];
+        d[k] = a - b;
+      }
+      C[i + j * ldc] = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    }
+}

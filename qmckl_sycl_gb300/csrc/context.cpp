@@ -256,6 +256,16 @@ const char* qmckl_string_of_error_device(const qmckl_exit_code_device error) {
     case QMCKL_INVALID_ARG_8_DEVICE: return "Invalid argument 8";
     case QMCKL_INVALID_ARG_9_DEVICE: return "Invalid argument 9";
     case QMCKL_INVALID_ARG_10_DEVICE: return "Invalid argument 10";
+    case QMCKL_INVALID_ARG_11_DEVICE: return "Invalid argument 11";
+    case QMCKL_INVALID_ARG_12_DEVICE: return "Invalid argument 12";
+    case QMCKL_INVALID_ARG_13_DEVICE: return "Invalid argument 13";
+    case QMCKL_INVALID_ARG_14_DEVICE: return "Invalid argument 14";
+    case QMCKL_INVALID_ARG_15_DEVICE: return "Invalid argument 15";
+    case QMCKL_INVALID_ARG_16_DEVICE: return "Invalid argument 16";
+    case QMCKL_INVALID_ARG_17_DEVICE: return "Invalid argument 17";
+    case QMCKL_INVALID_ARG_18_DEVICE: return "Invalid argument 18";
+    case QMCKL_INVALID_ARG_19_DEVICE: return "Invalid argument 19";
+    case QMCKL_INVALID_ARG_20_DEVICE: return "Invalid argument 20";
     case QMCKL_FAILURE_DEVICE: return "Failure";
     case QMCKL_ERRNO_DEVICE: return "Error (errno)";
     case QMCKL_INVALID_CONTEXT_DEVICE: return "Invalid context";

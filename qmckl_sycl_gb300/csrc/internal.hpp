@@ -105,6 +105,13 @@ struct WalkerData {
 struct ElectronData {
   int64_t num = 0, up_num = 0, down_num = 0;
   WalkerData walker, walker_old;
+  // cached distances (src/qmckl_electron.cpp:192-296 of the reference)
+  double* en_distance = nullptr;
+  size_t en_distance_cap = 0;
+  uint64_t en_distance_date = 0;
+  double* ee_distance = nullptr;
+  size_t ee_distance_cap = 0;
+  uint64_t ee_distance_date = 0;
   int32_t uninitialized = 0;
   bool provided = false;
 };

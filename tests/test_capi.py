@@ -67,6 +67,22 @@ def test_batch_argument_checks():
     assert L.qmckl_batch_get_launch_count_device(0) == 0
 
 
+def test_distance_argument_checks():
+    c = L.qmckl_context_create_device(0)
+    v = ctypes.c_void_p(1)  # never dereferenced: the checks fail first
+    assert L.qmckl_distance_device(c, b"T", b"T", 0, 4, v, 4, v, 4, v, 4) == 4
+    assert L.qmckl_distance_device(c, b"T", b"T", 4, 0, v, 4, v, 4, v, 4) == 5
+    assert L.qmckl_distance_device(c, b"X", b"T", 4, 4, v, 4, v, 4, v, 4) == 1
+    assert L.qmckl_distance_device(c, b"T", b"N", 4, 4, v, 3, v, 3, v, 4) == 7
+    assert L.qmckl_distance_device(c, b"N", b"T", 4, 4, v, 3, v, 3, v, 4) == 9
+    assert L.qmckl_distance_device(c, b"N", b"N", 4, 4, v, 3, v, 3, v, 3) == 11
+    assert L.qmckl_compute_en_distance_device(c, 0, 2, v, v, v) == 2
+    assert L.qmckl_compute_ee_distance_device(c, 2, 0, v, v) == 3
+    assert L.qmckl_distance_device(0, b"T", b"T", 4, 4, v, 4, v, 4, v, 4) == 103
+    assert L.qmckl_string_of_error_device(11) == b"Invalid argument 11"
+    assert L.qmckl_context_destroy_device(c) == 0
+
+
 def test_error_record_and_strings():
     c = L.qmckl_context_create_device(0)
     assert L.qmckl_context_check_device(c) == c
