@@ -288,10 +288,11 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_value_inplace_device(qmckl_context_
  * ====================================================================================== */
 
 /* MO contraction precision. FP64 (default, the drop-in) or a split-BF16 product on the
- * tcgen05 tensor cores (each FP64 operand split into three BF16 terms, six cross
- * products, FP32 accumulation folded into FP64). Distances, exponentials, screening and
- * the AO Laplacian assembly stay FP64 in both modes. Changing the mode touches the
- * context. */
+ * tcgen05 tensor cores (each operand split into three BF16 terms, six cross products, FP32
+ * accumulation with per-block two-sum folding). Distances, exponentials, radial sums,
+ * screening and the AO Laplacian assembly stay FP64 in both modes; in the split-BF16 mode the
+ * AO value and gradient are assembled in FP32 (the BF16 planes carry 24 significant bits).
+ * The AO getters always return the FP64 AOs. Changing the mode touches the context. */
 #define QMCKL_PRECISION_FP64_DEVICE 0
 #define QMCKL_PRECISION_SPLIT_BF16_DEVICE 1
 qmckl_exit_code_device qmckl_set_precision_mode_device(qmckl_context_device context, int32_t mode);

@@ -54,30 +54,42 @@ template <Out O>
 __host__ __device__ constexpr int ncomp() {
   return O == Out::Value ? 1 : 5;
 }
+// Resident CTAs per SM the register allocation must allow. The planes output stages nothing in
+// shared memory, so registers alone bound its occupancy: 6 CTAs (24 warps) per SM measured
+// 2.13 ms against 2.76 ms with the compiler's unconstrained allocation (4 CTAs) on the medium
+// workload. The staged ao_vgl output fits 5 CTAs in shared memory, ao_value 8 or more.
+template <Out O>
+__host__ __device__ constexpr int min_ctas() {
+  return O == Out::Planes ? 6 : (O == Out::Vgl ? 5 : 8);
+}
 
 // ---------------------------------------------------------------- output staging
 // Splits an FP64 value into three BF16 terms (hi + mid + lo carries 24 significant bits) with
 // integer and FP32 instructions only: FP64 -> FP32 by round-to-nearest-even on the bit pattern
 // (values below the FP32 normal range become zero, which is below the form's error budget).
-__device__ __forceinline__ void split_bf16x3(double a, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+__device__ __forceinline__ float f64_to_f32(double a) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(a);
   const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
   const int e = (int)((b >> 52) & 0x7FF) - 896;
-  float f;
-  if (e <= 0) {
-    f = __uint_as_float(sign);
-  } else {
-    const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
-    const unsigned int mm = (unsigned int)(frac >> 29);
-    const unsigned long long rem = frac & 0x1FFFFFFFull;
-    unsigned int bits = ((unsigned int)(e < 255 ? e : 255) << 23) | (e < 255 ? mm : 0u);
-    if (e < 255 && (rem > 0x10000000ull || (rem == 0x10000000ull && (mm & 1u)))) bits += 1u;
-    f = __uint_as_float(sign | bits);
-  }
+  if (e <= 0) return __uint_as_float(sign);
+  const unsigned long long frac = b & 0xFFFFFFFFFFFFFull;
+  const unsigned int mm = (unsigned int)(frac >> 29);
+  const unsigned long long rem = frac & 0x1FFFFFFFull;
+  unsigned int bits = ((unsigned int)(e < 255 ? e : 255) << 23) | (e < 255 ? mm : 0u);
+  if (e < 255 && (rem > 0x10000000ull || (rem == 0x10000000ull && (mm & 1u)))) bits += 1u;
+  return __uint_as_float(sign | bits);
+}
+
+// An FP32 value as three BF16 terms (exact: 24 significant bits).
+__device__ __forceinline__ void split_bf16x3f(float f, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
   h = __float2bfloat16_rn(f);
   const float r1 = f - __bfloat162float(h);
   m = __float2bfloat16_rn(r1);
   l = __float2bfloat16_rn(r1 - __bfloat162float(m));
+}
+
+__device__ __forceinline__ void split_bf16x3(double a, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
+  split_bf16x3f(f64_to_f32(a), h, m, l);
 }
 
 // Collects one warp's AO values (lane = point) for ao_vgl / ao_value and writes them as row
@@ -174,6 +186,22 @@ struct Writer<Out::Planes> {
     }
     fill += 1;
   }
+  // value and gradient already in FP32, Laplacian in FP64; drop: the AO's FP64 value is zero
+  __device__ __forceinline__ void emit_mixed(float v0, float gx, float gy, float gz, double lap, bool drop) {
+    if (lane < nvalid) {
+      __nv_bfloat16* o = planes + (int64_t)(base + fill) * row_len + slot;
+      const float vals[5] = {v0, drop ? 0.f : gx, drop ? 0.f : gy, drop ? 0.f : gz, drop ? 0.f : f64_to_f32(lap)};
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        __nv_bfloat16 h, m, l;
+        split_bf16x3f(vals[c], h, m, l);
+        o[c * pp] = h;
+        o[plane_stride + c * pp] = m;
+        o[2 * plane_stride + c * pp] = l;
+      }
+    }
+    fill += 1;
+  }
   __device__ __forceinline__ void emit_zeros(int count) {
     const double z[NC] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int i = 0; i < count; ++i) emit(z);
@@ -185,14 +213,57 @@ struct ShellVals {
   double R;    // radial value t0
   double t1, t2, t3;  // radial gradient = g * (x, y, z)
   double Rt;   // t4 + 2 l g, the radial part of the Laplacian after Euler's identity
+  float Rf, t1f, t2f, t3f;  // FP32 copies for the split-BF16 form's value and gradient
+};
+
+// Powers 0..3 of the displacement from the nucleus, FP64 and (split-BF16 form) FP32.
+struct Pows {
+  double X[4], Y[4], Z[4];
+  float Xf[4], Yf[4], Zf[4];
 };
 
 // One Cartesian component x^a y^b z^c (a, b, c compile-time), assembled like the
 // reference's src/qmckl_ao_sycl.cpp:371-420 and multiplied by the AO factor.
 template <Out O, int a, int b, int c>
-__device__ __forceinline__ void cart(Writer<O>& w, const double (&X)[4], const double (&Y)[4], const double (&Z)[4],
-                                     const ShellVals& s, double f, bool zero) {
+__device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVals& s, double f, bool zero) {
   constexpr int NC = ncomp<O>();
+  const double(&X)[4] = pw.X;
+  const double(&Y)[4] = pw.Y;
+  const double(&Z)[4] = pw.Z;
+  if constexpr (O == Out::Planes) {
+    // Split-BF16 form: the planes carry 24 significant bits, so the value and gradient are
+    // assembled in FP32; the Laplacian (cancellation-prone) in FP64 as in the FP64 form.
+    const float(&Xf)[4] = pw.Xf;
+    const float(&Yf)[4] = pw.Yf;
+    const float(&Zf)[4] = pw.Zf;
+    const float yzf = Yf[b] * Zf[c];
+    const float Pf = Xf[a] * yzf;
+    float gx = Pf * s.t1f, gy = Pf * s.t2f, gz = Pf * s.t3f;
+    if constexpr (a > 0) gx = fmaf((float)a * Xf[a - 1], yzf * s.Rf, gx);
+    if constexpr (b > 0) gy = fmaf((float)b * Yf[b - 1], (Xf[a] * Zf[c]) * s.Rf, gy);
+    if constexpr (c > 0) gz = fmaf((float)c * Zf[c - 1], (Xf[a] * Yf[b]) * s.Rf, gz);
+    float v0 = Pf * s.Rf;
+    const double yz = Y[b] * Z[c];
+    const double P = X[a] * yz;
+    double lap = P * s.Rt;
+    if constexpr (a > 1) lap = fma((double)(a * (a - 1)) * X[a - 2], yz * s.R, lap);
+    if constexpr (b > 1) lap = fma((double)(b * (b - 1)) * Y[b - 2], (X[a] * Z[c]) * s.R, lap);
+    if constexpr (c > 1) lap = fma((double)(c * (c - 1)) * Z[c - 2], (X[a] * Y[b]) * s.R, lap);
+    if (!is_one(f)) {
+      const float ff = f64_to_f32(f);
+      v0 *= ff;
+      gx *= ff;
+      gy *= ff;
+      gz *= ff;
+      lap *= f;
+    }
+    // the reference's MO kernel skips an AO whose FP64 value P R f is exactly zero
+    // (src/qmckl_mo_sycl.cpp:40): decided on the bits of the factors
+    const bool drop = zero || (bits_of(P) << 1) == 0 || (bits_of(s.R) << 1) == 0 || (bits_of(f) << 1) == 0;
+    if (zero) v0 = 0.f;
+    w.emit_mixed(v0, gx, gy, gz, lap, drop);
+    return;
+  }
   const double yz = Y[b] * Z[c];
   const double P = X[a] * yz;
   double v[NC];
@@ -229,33 +300,32 @@ __device__ __forceinline__ void cart(Writer<O>& w, const double (&X)[4], const d
 // Components of one shell in the reference's order: a descending, then b descending
 // (src/qmckl_ao_sycl.cpp:297-305).
 template <Out O, int L>
-__device__ __forceinline__ void shell_fixed(Writer<O>& w, const double (&X)[4], const double (&Y)[4],
-                                            const double (&Z)[4], const ShellVals& s, const double* __restrict__ aof,
-                                            int ao0, bool zero) {
+__device__ __forceinline__ void shell_fixed(Writer<O>& w, const Pows& pw, const ShellVals& s,
+                                            const double* __restrict__ aof, int ao0, bool zero) {
   if constexpr (L == 0) {
-    cart<O, 0, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0), zero);
+    cart<O, 0, 0, 0>(w, pw, s, __ldg(aof + ao0), zero);
   } else if constexpr (L == 1) {
-    cart<O, 1, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
-    cart<O, 0, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
-    cart<O, 0, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 1, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero);
+    cart<O, 0, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero);
+    cart<O, 0, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero);
   } else if constexpr (L == 2) {
-    cart<O, 2, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
-    cart<O, 1, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
-    cart<O, 1, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
-    cart<O, 0, 2, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 3), zero);
-    cart<O, 0, 1, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 4), zero);
-    cart<O, 0, 0, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 5), zero);
+    cart<O, 2, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero);
+    cart<O, 1, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero);
+    cart<O, 1, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 0, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero);
+    cart<O, 0, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero);
+    cart<O, 0, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero);
   } else {
-    cart<O, 3, 0, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 0), zero);
-    cart<O, 2, 1, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 1), zero);
-    cart<O, 2, 0, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 2), zero);
-    cart<O, 1, 2, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 3), zero);
-    cart<O, 1, 1, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 4), zero);
-    cart<O, 1, 0, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 5), zero);
-    cart<O, 0, 3, 0>(w, X, Y, Z, s, __ldg(aof + ao0 + 6), zero);
-    cart<O, 0, 2, 1>(w, X, Y, Z, s, __ldg(aof + ao0 + 7), zero);
-    cart<O, 0, 1, 2>(w, X, Y, Z, s, __ldg(aof + ao0 + 8), zero);
-    cart<O, 0, 0, 3>(w, X, Y, Z, s, __ldg(aof + ao0 + 9), zero);
+    cart<O, 3, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero);
+    cart<O, 2, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero);
+    cart<O, 2, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 1, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero);
+    cart<O, 1, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero);
+    cart<O, 1, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero);
+    cart<O, 0, 3, 0>(w, pw, s, __ldg(aof + ao0 + 6), zero);
+    cart<O, 0, 2, 1>(w, pw, s, __ldg(aof + ao0 + 7), zero);
+    cart<O, 0, 1, 2>(w, pw, s, __ldg(aof + ao0 + 8), zero);
+    cart<O, 0, 0, 3>(w, pw, s, __ldg(aof + ao0 + 9), zero);
   }
 }
 
@@ -348,17 +418,33 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
       w.emit_zeros(N.ao_end - N.ao_begin);
       continue;
     }
-    double X[4], Y[4], Z[4];
-    X[0] = Y[0] = Z[0] = 1.0;
-    X[1] = x;
-    Y[1] = y;
-    Z[1] = z;
-    X[2] = X[1] * x;
-    Y[2] = Y[1] * y;
-    Z[2] = Z[1] * z;
-    X[3] = X[2] * x;
-    Y[3] = Y[2] * y;
-    Z[3] = Z[2] * z;
+    Pows pw;
+    pw.X[0] = pw.Y[0] = pw.Z[0] = 1.0;
+    pw.X[1] = x;
+    pw.Y[1] = y;
+    pw.Z[1] = z;
+    pw.X[2] = pw.X[1] * x;
+    pw.Y[2] = pw.Y[1] * y;
+    pw.Z[2] = pw.Z[1] * z;
+    pw.X[3] = pw.X[2] * x;
+    pw.Y[3] = pw.Y[2] * y;
+    pw.Z[3] = pw.Z[2] * z;
+    float xf = 0.f, yf = 0.f, zf = 0.f;
+    if constexpr (O == Out::Planes) {
+      xf = f64_to_f32(x);
+      yf = f64_to_f32(y);
+      zf = f64_to_f32(z);
+      pw.Xf[0] = pw.Yf[0] = pw.Zf[0] = 1.f;
+      pw.Xf[1] = xf;
+      pw.Yf[1] = yf;
+      pw.Zf[1] = zf;
+      pw.Xf[2] = xf * xf;
+      pw.Yf[2] = yf * yf;
+      pw.Zf[2] = zf * zf;
+      pw.Xf[3] = pw.Xf[2] * xf;
+      pw.Yf[3] = pw.Yf[2] * yf;
+      pw.Zf[3] = pw.Zf[2] * zf;
+    }
     for (int si = N.shell_begin; si < N.shell_end; ++si) {
       const ShellEntry S = a.shells[si];
       double t0 = 0.0, g = 0.0, h = 0.0;
@@ -380,7 +466,17 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
       }
       ShellVals sv;
       sv.R = t0;
-      if constexpr (NC == 5) {
+      if constexpr (O == Out::Planes) {
+        // FP32 value/gradient inputs; the radial part of the Laplacian stays FP64
+        const float gf = f64_to_f32(g);
+        sv.Rf = f64_to_f32(t0);
+        sv.t1f = gf * xf;
+        sv.t2f = gf * yf;
+        sv.t3f = gf * zf;
+        sv.t1 = sv.t2 = sv.t3 = 0.0;
+        const double t4 = fma(-2.0, h, 3.0 * g);
+        sv.Rt = fma((double)(2 * S.l), g, t4);
+      } else if constexpr (NC == 5) {
         sv.t1 = g * x;
         sv.t2 = g * y;
         sv.t3 = g * z;
@@ -390,11 +486,18 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
         sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
       }
       switch (S.l) {
-        case 0: shell_fixed<O, 0>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
-        case 1: shell_fixed<O, 1>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
-        case 2: shell_fixed<O, 2>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
-        case 3: shell_fixed<O, 3>(w, X, Y, Z, sv, a.aof, S.ao_begin, scr); break;
-        default: shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr); break;
+        case 0: shell_fixed<O, 0>(w, pw, sv, a.aof, S.ao_begin, scr); break;
+        case 1: shell_fixed<O, 1>(w, pw, sv, a.aof, S.ao_begin, scr); break;
+        case 2: shell_fixed<O, 2>(w, pw, sv, a.aof, S.ao_begin, scr); break;
+        case 3: shell_fixed<O, 3>(w, pw, sv, a.aof, S.ao_begin, scr); break;
+        default:
+          if constexpr (O == Out::Planes) {  // the generic path assembles in FP64
+            sv.t1 = g * x;
+            sv.t2 = g * y;
+            sv.t3 = g * z;
+          }
+          shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
+          break;
       }
     }
   }
@@ -407,7 +510,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
 
 // One molecule: warp task = blockIdx.x * kWarps + warp.
 template <Out O>
-__global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a) {
+__global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(const FusedArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* thi = reinterpret_cast<double*>(smem_raw);
   double* tlo = thi + 32;
@@ -422,7 +525,7 @@ __global__ void __launch_bounds__(kWarps * 32) ao_fused_kernel(const FusedArgs a
 // Many molecules, persistent: each warp takes the next task from a global counter until the
 // tasks of every molecule are done (uneven molecules balance themselves).
 template <Out O>
-__global__ void __launch_bounds__(kWarps * 32) ao_batch_kernel(const FusedArgs* __restrict__ mols,
+__global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(const FusedArgs* __restrict__ mols,
                                                                 const int64_t* __restrict__ task_begin, int nmol,
                                                                 int64_t total, unsigned long long* counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
