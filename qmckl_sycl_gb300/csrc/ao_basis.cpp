@@ -295,7 +295,7 @@ const int32_t* point_order(Ctx* ctx) {
   ao.point_perm = static_cast<int32_t*>(perm);
   ao.point_keys = static_cast<int32_t*>(keys);
   ao.cell_counts = static_cast<int32_t*>(counts);
-  if (launch_point_order(ctx, ao.tables, ctx->point.coord, P, ao.point_keys, ao.cell_counts, ao.point_perm) !=
+  if (launch_point_order(ctx, ao.tables, ctx->point.coord, P, P, ao.point_keys, ao.cell_counts, ao.point_perm) !=
       cudaSuccess)
     return nullptr;
   ao.perm_date = ctx->point.date;

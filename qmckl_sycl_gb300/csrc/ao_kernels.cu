@@ -386,7 +386,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   const int64_t slot = p0 + (lane < nvalid ? lane : nvalid - 1);
   const int64_t p = a.perm ? (int64_t)a.perm[slot] : slot;
   const int64_t P = a.point_num;
-  const double ex = a.coord[p], ey = a.coord[P + p], ez = a.coord[2 * P + p];
+  const double ex = a.coord[p], ey = a.coord[a.coord_ld + p], ez = a.coord[2 * a.coord_ld + p];
 
   Writer<O> w;
   w.st = st;
@@ -596,12 +596,12 @@ __global__ void shell_vgl_kernel(const NucleusEntry* __restrict__ nuclei, const 
 __device__ __forceinline__ int morton_key(double x, double y, double z, const double* origin, double inv_cell);
 
 // 15-bit Morton key of a point's cell on the 32^3 grid; one counter per cell.
-__global__ void morton_key_kernel(const double* __restrict__ coord, int64_t P, double ox, double oy, double oz,
-                                  double inv_cell, int32_t* __restrict__ keys, int32_t* __restrict__ counts) {
+__global__ void morton_key_kernel(const double* __restrict__ coord, int64_t ld, int64_t P, double ox, double oy,
+                                  double oz, double inv_cell, int32_t* __restrict__ keys, int32_t* __restrict__ counts) {
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const double origin[3] = {ox, oy, oz};
-  const int key = morton_key(coord[p], coord[P + p], coord[2 * P + p], origin, inv_cell);
+  const int key = morton_key(coord[p], coord[ld + p], coord[2 * ld + p], origin, inv_cell);
   keys[p] = key;
   atomicAdd(&counts[key], 1);
 }
@@ -662,10 +662,11 @@ size_t fused_smem() {
 
 template <Out O>
 cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
-                         double* out, __nv_bfloat16* planes, int64_t row_len, const char* name) {
+                         double* out, __nv_bfloat16* planes, int64_t row_len, const char* name, int64_t coord_ld = -1) {
   if (point_num <= 0 || t.ao_num <= 0) return cudaSuccess;
   const int64_t groups = (point_num + 31) / 32;
-  const FusedArgs a = make_fused_args(t, pick_level(t, groups, t.sm_count), coord, perm, point_num, out, planes, row_len);
+  FusedArgs a = make_fused_args(t, pick_level(t, groups, t.sm_count), coord, perm, point_num, out, planes, row_len);
+  if (coord_ld >= 0) a.coord_ld = coord_ld;
   const int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
   const size_t smem = fused_smem<O>();
   cudaFuncSetAttribute(ao_fused_kernel<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -744,6 +745,7 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.ao_num = t.ao_num;
   a.row_len = row_len;
   a.plane_pp = (point_num + 31) / 32 * 32;
+  a.coord_ld = point_num;
   a.task_num = ((point_num + 31) / 32) * a.chunk_num;
   return a;
 }
@@ -794,15 +796,15 @@ cudaError_t launch_order_batch(cudaStream_t stream, const OrderDesc* desc, const
   return cudaGetLastError();
 }
 
-cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int32_t* keys,
-                               int32_t* counts, int32_t* perm) {
+cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t coord_ld, int64_t point_num,
+                               int32_t* keys, int32_t* counts, int32_t* perm) {
   if (point_num <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * kOrderCells, ctx->stream);
   if (e != cudaSuccess) return e;
   const unsigned blocks = (unsigned)((point_num + 255) / 256);
   {
     LaunchScope scope(ctx, "point_order_keys");
-    morton_key_kernel<<<blocks, 256, 0, ctx->stream>>>(coord, point_num, t.grid_origin[0], t.grid_origin[1],
+    morton_key_kernel<<<blocks, 256, 0, ctx->stream>>>(coord, coord_ld, point_num, t.grid_origin[0], t.grid_origin[1],
                                                        t.grid_origin[2], t.grid_inv_cell, keys, counts);
   }
   {
@@ -824,10 +826,10 @@ cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, co
   return launch_fused<Out::Value>(ctx, t, coord, perm, point_num, ao_value, nullptr, t.ao_num, "ao_value_fused");
 }
 
-cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
+cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, int64_t coord_ld, const int32_t* perm,
                              int64_t point_num, int64_t kp, void* planes) {
   return launch_fused<Out::Planes>(ctx, t, coord, perm, point_num, nullptr, static_cast<__nv_bfloat16*>(planes), kp,
-                                   "ao_vgl_fused_bf16_planes");
+                                   "ao_vgl_fused_bf16_planes", coord_ld);
 }
 
 cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int64_t shell_num,

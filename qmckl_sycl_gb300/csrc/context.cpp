@@ -212,6 +212,7 @@ qmckl_exit_code_device qmckl_context_destroy_device(const qmckl_context_device c
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   cudaGetLastError();
   ctx->tag = kInvalidTag;
   delete ctx;

@@ -208,6 +208,7 @@ struct qmckl_context_struct_device {
   int32_t device_id = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  cudaStream_t copy_stream = nullptr;  // device-to-host copies overlapped with compute
   bool async = false;
   int32_t precision = QMCKL_PRECISION_FP64_DEVICE;
 
@@ -290,8 +291,8 @@ struct LaunchScope {
 constexpr int kOrderCells = 32 * 32 * 32;
 // perm <- an order of the points that puts spatial neighbours in the same warp (counting
 // sort of their Morton cell keys); keys [P] and counts [kOrderCells] are scratch.
-cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num, int32_t* keys,
-                               int32_t* counts, int32_t* perm);
+cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t coord_ld, int64_t point_num,
+                               int32_t* keys, int32_t* counts, int32_t* perm);
 // Fused AO kernels; perm (may be null) is the processing order of the points.
 cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
                           double* ao_vgl);
@@ -301,7 +302,7 @@ cudaError_t launch_ao_value(Ctx* ctx, const AoTables& t, const double* coord, co
 // planes [3][kp][5 pp] with pp = point_num rounded up to 32, operand row c * pp + s holding
 // component c of the point at processing slot s (perm order); AOs [ao_num, kp) are zero and
 // the reference's zero-value skip is applied.
-cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm,
+cudaError_t launch_ao_planes(Ctx* ctx, const AoTables& t, const double* coord, int64_t coord_ld, const int32_t* perm,
                              int64_t point_num, int64_t kp, void* planes);
 cudaError_t launch_shell_vgl(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num,
                              int64_t shell_num, double* shell_vgl);
@@ -330,7 +331,7 @@ struct FusedArgs {
   const double* aof;
   const NucleusChunk* chunks;
   const ExpTable* exp_table;
-  const double* coord;      // [3][P]
+  const double* coord;      // [3][coord_ld]: x of point p at coord[p], y at coord[coord_ld + p], ...
   const int32_t* perm;      // processing order of the points, or null
   double* out;              // ao_vgl (FP64 output)
   void* planes;             // BF16 planes [3][row_len][5 plane_pp], M-major (split-BF16 output)
@@ -338,6 +339,7 @@ struct FusedArgs {
   int64_t ao_num;
   int64_t row_len;          // ao_num, or the padded K of the planes
   int64_t plane_pp;         // points rounded up to a multiple of 32
+  int64_t coord_ld;         // row stride of coord (point_num, or more for a slice of a larger set)
   int64_t task_num;
   int chunk_num;
 };
@@ -392,6 +394,9 @@ int split_make_job_mn(void* job_host, const void* a_planes, int64_t pp, int64_t 
                       const void* b_planes, int64_t M, int64_t kp, double* out, int tile_begin, int n_cap);
 cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, int total_tiles, int* err);
 int64_t split_k_pad(int64_t ao_num);
+// mo_vgl of the split-BF16 form computed in `chunks` point ranges whose results are copied to the
+// host buffer while the next range computes (the cache ends up holding the full result).
+qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks);
 // The member's coefficient planes for the split-BF16 form (built once per coefficient set)
 // and its AO-plane buffer for rows x kp (returns null on allocation failure).
 qmckl_exit_code_device split_prepare_coef(Ctx* ctx, qmckl_context_device c, int64_t kp);

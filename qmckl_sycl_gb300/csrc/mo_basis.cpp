@@ -199,10 +199,31 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
   return QMCKL_SUCCESS_DEVICE;
 }
 
+// True for host memory (page-locked or not): a destination the device reaches over the host link.
+static bool host_memory(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeUnregistered;
+}
+
 qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device context, double* const mo_vgl,
                                                         const int64_t size_max) {
   Ctx* ctx = checked(context);
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
+  MoBasisData& mo = ctx->mo_basis;
+  // split-BF16 results for a host buffer on a large point set: compute in chunks and overlap the
+  // device-to-host copy of each chunk with the next chunk's compute
+  if (mo.provided && ctx->ao_basis.provided && ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE &&
+      ctx->point.date > mo.mo_vgl_date && ctx->point.num >= 16384 && mo_vgl &&
+      size_max >= 5 * ctx->point.num * mo.mo_num && ensure_device(ctx) && host_memory(mo_vgl)) {
+    qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, 4);
+    if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+    mo.mo_vgl_date = ctx->date;
+    return QMCKL_SUCCESS_DEVICE;
+  }
   qmckl_exit_code_device rc = qmckl_provide_mo_basis_mo_vgl_device(context);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
   const int64_t sze = 5 * ctx->point.num * ctx->mo_basis.mo_num;

@@ -813,7 +813,7 @@ static qmckl_exit_code_device split_mo_vgl(Ctx* ctx, qmckl_context_device c, dou
   if (!err) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
   __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(ctx->mo_basis.ao_split);
   const int32_t* perm = point_order(ctx);
-  launch_ao_planes(ctx, ctx->ao_basis.tables, ctx->point.coord, perm, P, kp, ap);
+  launch_ao_planes(ctx, ctx->ao_basis.tables, ctx->point.coord, P, perm, P, kp, ap);
   SplitJob job;
   const int tiles = make_job_mn(job, ap, pp, P, perm, static_cast<const __nv_bfloat16*>(ctx->mo_basis.coef_split),
                                 M, kp, out, 0);
@@ -846,6 +846,87 @@ qmckl_exit_code_device split_prepare_coef(Ctx* ctx, qmckl_context_device c, int6
 
 void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
   return ensure_a_planes(ctx, rows, kp) ? ctx->mo_basis.ao_split : nullptr;
+}
+
+// mo_vgl of the split-BF16 form for a caller's host buffer: the points are processed in chunks
+// (contiguous point ranges, each ordered on its own) whose rows of the cached mo_vgl are copied to
+// the host on a second stream while the next chunk computes, so the device-to-host transfer (~190
+// GB/s over the host link here, 2.6 ms for the medium workload's 491 MB) overlaps the compute.
+qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks) {
+  const char* fn = "qmckl_get_mo_basis_mo_vgl_device";
+  const int64_t P = ctx->point.num, A = ctx->ao_basis.ao_num, M = ctx->mo_basis.mo_num;
+  MoBasisData& mo = ctx->mo_basis;
+  AoBasisData& ao = ctx->ao_basis;
+  const int64_t kp = round_up(A, kBK);
+  chunks = chunks < 1 ? 1 : (chunks > 16 ? 16 : chunks);
+  const int64_t pc = round_up((P + chunks - 1) / chunks, 32);  // points per chunk
+  if (5 * pc > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
+  qmckl_exit_code_device rc = ensure_tables(ctx, c);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  rc = ensure_coef_planes(ctx, c, kp);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  if (!ensure(ctx, &mo.mo_vgl, &mo.mo_vgl_cap, sizeof(double) * 5 * M * P))
+    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "mo_vgl");
+  int* err = ensure_a_planes(ctx, 5 * pc, kp);
+  if (!err) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split AO planes");
+  void* perm = ao.point_perm;
+  void* keys = ao.point_keys;
+  void* counts = ao.cell_counts;
+  const bool ok = ensure_raw(ctx, &perm, &ao.perm_cap, sizeof(int32_t) * pc) &&
+                  ensure_raw(ctx, &keys, &ao.keys_cap, sizeof(int32_t) * pc) &&
+                  ensure_raw(ctx, &counts, &ao.counts_cap, sizeof(int32_t) * kOrderCells);
+  ao.point_perm = static_cast<int32_t*>(perm);
+  ao.point_keys = static_cast<int32_t*>(keys);
+  ao.cell_counts = static_cast<int32_t*>(counts);
+  ao.perm_date = 0;  // the buffer holds chunk-local orders from here on
+  if (!ok) return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "point order buffers");
+  if (!ctx->copy_stream && cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, QMCKL_FAILURE_DEVICE, fn, "stream creation failed");
+  }
+  if (!ensure_raw(ctx, &mo.split_job, &mo.split_job_cap, sizeof(SplitJob)))
+    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptor");
+  __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
+  cudaEvent_t done[16];
+  const int nc = (int)((P + pc - 1) / pc);
+  for (int k = 0; k < nc; ++k) cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < nc && e == cudaSuccess; ++k) {
+    const int64_t off = k * pc, n = P - off < pc ? P - off : pc;
+    const double* coord = ctx->point.coord + off;  // rows of [3][P], slice of n points
+    launch_point_order(ctx, ao.tables, coord, P, n, ao.point_keys, ao.cell_counts, ao.point_perm);
+    launch_ao_planes(ctx, ao.tables, coord, P, ao.point_perm, n, kp, ap);
+    SplitJob job;
+    const int tiles = make_job_mn(job, ap, round_up(n, 32), n, ao.point_perm,
+                                  static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
+    if (tiles < 0) {
+      e = cudaErrorInvalidValue;
+      break;
+    }
+    // the descriptor upload is ordered after the previous chunk's contraction on this stream
+    e = cudaMemcpyAsync(mo.split_job, &job, sizeof job, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) break;
+    {
+      LaunchScope scope(ctx, "mo_vgl_split_bf16");
+      launch_split_jobs(ctx->stream, static_cast<const SplitJob*>(mo.split_job), 1, tiles, err);
+    }
+    cudaEventRecord(done[k], ctx->stream);
+    cudaStreamWaitEvent(ctx->copy_stream, done[k], 0);
+    e = cudaMemcpyAsync(host_dst + 5 * off * M, mo.mo_vgl + 5 * off * M, sizeof(double) * 5 * n * M,
+                        cudaMemcpyDeviceToHost, ctx->copy_stream);
+  }
+  cudaError_t e2 = cudaStreamSynchronize(ctx->copy_stream);
+  cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
+  for (int k = 0; k < nc; ++k) cudaEventDestroy(done[k]);
+  if (e == cudaSuccess) e = e2 != cudaSuccess ? e2 : e3;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, QMCKL_FAILURE_DEVICE, fn, cudaGetErrorString(e));
+  }
+  int h = 0;
+  cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (h) return fail(c, QMCKL_FAILURE_DEVICE, fn, "split-BF16 GEMM: a pipeline wait timed out");
+  return QMCKL_SUCCESS_DEVICE;
 }
 
 qmckl_exit_code_device provide_mo_split(Ctx* ctx, qmckl_context_device c, double* dst, bool value_only) {

@@ -68,3 +68,25 @@ def test_split_tile_edges(mo_num):
     ref = oracle.forward(s, want=("mo_vgl",))
     out = run(s, PRECISION_SPLIT_BF16)
     assert normwise_rel_err(out["mo_vgl"], ref["mo_vgl"]) <= MIXED_RTOL
+
+
+def test_host_getter_overlaps_copies_bitwise():
+    # >= 16384 points and a host buffer: computed in point-range chunks whose rows are copied to
+    # the host while the next chunk computes; the result must equal the one-pass device result
+    import ctypes
+
+    s = config_medium(0, walkers=104, electrons=160)  # 16640 points
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(PRECISION_SPLIT_BF16)
+        P, M = s.point_num, s.mo_num
+        host = ctx.get_mo_vgl(P)  # pipelined path (numpy buffer is host memory)
+        dev = ctx.buffer("mo", 8 * 5 * P * M)
+        ctx.call("get_mo_basis_mo_vgl_inplace", dev.ptr, 5 * P * M)  # one pass, device buffer
+        one_pass = ctx.download(dev.ptr, (P, 5, M))
+        again = ctx.get_mo_vgl(P)  # cached: plain copy
+    assert np.array_equal(host, one_pass)
+    assert np.array_equal(again, host)
+    idx = np.arange(0, P, 97)
+    ref = oracle.forward(s.with_points(s.coord[idx]), want=("mo_vgl",))["mo_vgl"]
+    assert normwise_rel_err(host[idx], ref) <= MIXED_RTOL
