@@ -38,7 +38,7 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=100)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--form", choices=["fp64", "mixed"], default=None)
@@ -91,7 +91,7 @@ class Dist:
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled every 50 ms during a timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -105,10 +105,15 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once nvidia-smi is sampling
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 3.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.skip = len(self.lines)
         except OSError:
             self.proc = None
         return self
@@ -128,7 +133,7 @@ class ClockSampler:
     def summary(self):
         sm, smax, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in self.lines[getattr(self, "skip", 0):]:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
@@ -466,13 +471,15 @@ def main():
     headline = args.form or ("mixed" if "mixed" in forms else "fp64")
 
     results = {}
-    clocks = ClockSampler(dist.local_rank)
+    samplers = {f: ClockSampler(dist.local_rank) for f in forms}
+    clocks = samplers[headline]
     for form in forms:
-        ms, stats, launches = time_form(ctx, s, form, args.steps, args.warmup, dist,
-                                        clocks if form == headline else None)
+        # the FP64 form (150 ms a step) is timed on at most 10 steps when it is not the headline
+        k = args.steps if form == headline else min(args.steps, 10)
+        ms, stats, launches = time_form(ctx, s, form, k, args.warmup, dist, samplers[form])
         t = dist.max(ms)
-        total_points = dist.sum(P * args.steps)
-        results[form] = dict(ms=t, value=total_points / (t * 1e-3), stats=stats, launches=launches)
+        total_points = dist.sum(P * k)
+        results[form] = dict(ms=t, value=total_points / (t * 1e-3), stats=stats, launches=launches, steps=k)
 
     # accuracy of the mixed form against the FP64 form on the same inputs
     acc = None
@@ -551,8 +558,9 @@ def main():
         "roofline": roofline, "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": hr["launches"], "clocks": clocks.summary(),
-        "forms": {f: {"value": results[f]["value"], "ms_per_step": results[f]["ms"] / args.steps,
-                      "kernels": rf[f]} for f in forms},
+        "clocks_by_form": {f: samplers[f].summary() for f in forms},
+        "forms": {f: {"value": results[f]["value"], "ms_per_step": results[f]["ms"] / results[f]["steps"],
+                      "steps": results[f]["steps"], "kernels": rf[f]} for f in forms},
         "fp64_peak_tflops": fp64_peak.value,
     }
     if acc:
