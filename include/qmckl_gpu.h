@@ -337,6 +337,14 @@ qmckl_exit_code_device qmckl_measure_fp64_peak_device(qmckl_context_device conte
  * basis (QMCKL_NOT_PROVIDED_DEVICE otherwise). */
 qmckl_exit_code_device qmckl_exp_check_device(qmckl_context_device context, const double* x, int64_t n, double* out);
 
+/* Validation of the primitive values the split-BF16 form's AO kernel computes: for a device
+ * array r2[n] of squared distances, writes out[i][k] = coefficient_normalized[k] *
+ * e^(-exponent[k] r2[i]) as that kernel evaluates it, or 0 where the primitive is screened
+ * (exponent[k] r2[i] > 27.631021115928547), for every primitive k < prim_num (out: device,
+ * n * prim_num doubles). Needs a finalized AO basis (QMCKL_NOT_PROVIDED_DEVICE otherwise). */
+qmckl_exit_code_device qmckl_prim_value_check_device(qmckl_context_device context, const double* r2, int64_t n,
+                                                     double* out, int64_t size_max);
+
 /* Split-BF16 MO contraction that allocates nothing (no counterpart in the reference).
  *
  *   out[r][m] = sum_k ao[r][k] * coefficient[m][k]      (r < rows, m < mo_num)

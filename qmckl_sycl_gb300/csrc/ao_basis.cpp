@@ -71,7 +71,9 @@ void free_tables(Ctx* ctx, AoTables& t) {
   dfree(ctx, t.prim_orig);
   dfree(ctx, t.chunks);
   dfree(ctx, t.exp_table);
+  dfree(ctx, t.fold);
   t.exp_table = nullptr;
+  t.fold = nullptr;
   t.nuclei = nullptr;
   t.shells = nullptr;
   t.prims = nullptr;
@@ -136,6 +138,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   t.h_nuclei.clear();
   t.h_shells.clear();
   t.h_prims.clear();
+  t.h_fold.clear();
   t.h_chunks.clear();
   t.h_shell_orig.clear();
   t.h_prim_orig.clear();
@@ -209,6 +212,32 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
     et[0].hi[j] = (double)v;
     et[0].lo[j] = (double)(v - (long double)et[0].hi[j]);
   }
+  for (int j = 0; j < 256; ++j) et[0].fine[j] = (double)exp2l((long double)j / 256.0L);
+  // the split-BF16 form's folded primitives: every exponent positive and finite, every
+  // coefficient zero or of binary exponent within +-900 (so that sign * 2^k * e^y stays a
+  // normal double over the active range y in [-27.7, ln 2))
+  bool fold_ok = true;
+  t.h_fold.resize(t.h_prims.size());
+  for (size_t i = 0; i < t.h_prims.size(); ++i) {
+    const PrimEntry& pe = t.h_prims[i];
+    PrimFold& f = t.h_fold[i];
+    f = PrimFold{};
+    if (!(pe.expo > 0.0) || !(pe.expo < 1e150) || !std::isfinite(pe.coef)) fold_ok = false;
+    f.thr_bits = pe.coef == 0.0 ? 0 : pe.thr_bits;
+    f.na = -pe.expo;
+    f.m2a = pe.m2a;
+    f.m2a2 = -2.0 * (pe.expo * pe.expo);
+    if (pe.coef != 0.0 && std::isfinite(pe.coef)) {
+      int e2 = 0;
+      const double m = std::frexp(std::fabs(pe.coef), &e2);  // |coef| = m 2^e2, m in [0.5, 1)
+      f.k = e2 - 1;
+      f.lnm = std::log(2.0 * m);
+      f.sign = std::signbit(pe.coef) ? 0x80000000u : 0u;
+      if (f.k < -900 || f.k > 900) fold_ok = false;
+    }
+    f.naf = (float)f.na;
+    f.lnmf = (float)f.lnm;
+  }
   // point-grouping grid over the nuclei plus a 4-bohr margin, 32 cells along the longest side
   {
     double lo[3] = {HUGE_VAL, HUGE_VAL, HUGE_VAL}, hi[3] = {-HUGE_VAL, -HUGE_VAL, -HUGE_VAL};
@@ -253,6 +282,13 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   }
   t.chunks = to_device(ctx, t.h_chunks);
   t.exp_table = to_device(ctx, et);
+  if (fold_ok && !t.h_fold.empty()) {
+    t.fold = to_device(ctx, t.h_fold);
+    if (!t.fold) {
+      free_tables(ctx, t);
+      return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "kernel tables");
+    }
+  }
   if (!t.nuclei || !t.shells || !t.prims || !t.ao_factor || !t.shell_orig || !t.shell_nucl || !t.chunks ||
       !t.exp_table || (!t.h_prim_orig.empty() && !t.prim_orig)) {
     free_tables(ctx, t);

@@ -63,6 +63,13 @@ __host__ __device__ constexpr int min_ctas() {
   return O == Out::Planes ? 6 : (O == Out::Vgl ? 5 : 8);
 }
 
+// Dynamic shared memory: the exponential's tables (2 x 32 doubles, plus the 256-entry table
+// of the split-BF16 form), then the per-warp staging buffers.
+template <Out O>
+__host__ __device__ constexpr size_t stage_offset() {
+  return O == Out::Planes ? 512 + 2048 : 512;
+}
+
 // ---------------------------------------------------------------- output staging
 // Splits an FP64 value into three BF16 terms (hi + mid + lo carries 24 significant bits) with
 // integer and FP32 instructions only: FP64 -> FP32 by round-to-nearest-even on the bit pattern
@@ -90,6 +97,43 @@ __device__ __forceinline__ void split_bf16x3f(float f, __nv_bfloat16& h, __nv_bf
 
 __device__ __forceinline__ void split_bf16x3(double a, __nv_bfloat16& h, __nv_bfloat16& m, __nv_bfloat16& l) {
   split_bf16x3f(f64_to_f32(a), h, m, l);
+}
+
+// -n as a double, exactly, with integer instructions only (n = 0 gives 0).
+__device__ __forceinline__ double neg_int_to_double(int n) {
+  const unsigned u = n < 0 ? 0u - (unsigned)n : (unsigned)n;
+  const int msb = 31 - __clz(u);
+  // the mantissa's leading bit carries into the exponent field: (1022 + msb) + 1
+  const unsigned long long b = ((unsigned long long)(1022 + msb) << 52) + ((unsigned long long)u << (52 - msb));
+  const unsigned long long sg = n > 0 ? 0x8000000000000000ull : 0ull;
+  return u == 0 ? 0.0 : __longlong_as_double((long long)(b | sg));
+}
+
+constexpr float kInvL256f = 369.32993f;                  // 256 / ln 2 (only picks the table index)
+constexpr double kL256 = 0.6931471805599453094 / 256.0;  // double nearest ln 2, / 256 (exact)
+
+// One primitive of the split-BF16 form: v = coef * e^(-expo r2) = sign * 2^k * e^y with
+// y = ln(mant) - expo r2 in FP64 (one fused multiply-add). e^y = 2^(n>>8) 2^((n&255)/256) e^r,
+// r = y - n ln2/256: n comes from an FP32 estimate of y (|r| <= ln2/512 + 1e-5 on the active
+// range y in [-27.7, ln 2)), -n is formed exactly with integer instructions, e^r - 1 by a
+// degree-4 polynomial (truncation 4e-17), 2^(j/256) from a 256-entry table, and the power of
+// two and the sign by integer addition: 9 FP64 instructions against 14 for coef * e^-(expo r2)
+// with the 32-entry method. The relative error stays within a few units of 1e-16 |y|.
+__device__ __forceinline__ double fold_value(const PrimFold* __restrict__ F, double r2, float r2f,
+                                             const double* __restrict__ fine) {
+  const float yf = fmaf(__ldg(&F->naf), r2f, __ldg(&F->lnmf));
+  const float tf = fmaf(yf, kInvL256f, 12582912.0f);  // 1.5 * 2^23: rounds to an integer
+  const int n = __float_as_int(tf) - 0x4B400000;
+  const double y = fma(__ldg(&F->na), r2, __ldg(&F->lnm));
+  const double r = fma(neg_int_to_double(n), kL256, y);
+  double q = fma(r, 1.0 / 24.0, 1.0 / 6.0);
+  q = fma(q, r, 0.5);
+  const double p = fma(r * r, q, r);  // e^r - 1
+  const double th = fine[n & 255];
+  const double e = fma(th, p, th);
+  const unsigned long long m = (unsigned long long)(long long)((n >> 8) + __ldg(&F->k));
+  const unsigned long long b = (unsigned long long)__double_as_longlong(e) + (m << 52);
+  return __longlong_as_double((long long)(b ^ ((unsigned long long)__ldg(&F->sign) << 32)));
 }
 
 // Collects one warp's AO values (lane = point) for ao_vgl / ao_value and writes them as row
@@ -376,7 +420,8 @@ __device__ __noinline__ void shell_generic(Writer<O>& w, double x, double y, dou
 // One warp task: 32 points (lane = point) x one chunk of consecutive nuclei.
 template <Out O>
 __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
-                                        const double* __restrict__ thi, const double* __restrict__ tlo, int lane) {
+                                        const double* __restrict__ thi, const double* __restrict__ tlo,
+                                        const double* __restrict__ fine, int lane) {
   constexpr int NC = ncomp<O>();
   const int64_t group = task / a.chunk_num;
   const int ch = (int)(task - group * a.chunk_num);
@@ -429,8 +474,11 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     pw.X[3] = pw.X[2] * x;
     pw.Y[3] = pw.Y[2] * y;
     pw.Z[3] = pw.Z[2] * z;
-    float xf = 0.f, yf = 0.f, zf = 0.f;
+    float xf = 0.f, yf = 0.f, zf = 0.f, r2f = 0.f;
+    double m2r2 = 0.0;
     if constexpr (O == Out::Planes) {
+      r2f = f64_to_f32(r2);
+      m2r2 = -2.0 * r2;
       xf = f64_to_f32(x);
       yf = f64_to_f32(y);
       zf = f64_to_f32(z);
@@ -448,34 +496,58 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     for (int si = N.shell_begin; si < N.shell_end; ++si) {
       const ShellEntry S = a.shells[si];
       double t0 = 0.0, g = 0.0, h = 0.0;
-      for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
-        const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
-        if (__any_sync(kFull, act)) {
-          const double expo = __ldg(&a.prims[pi].expo);
-          const double ar2 = expo * r2;
-          const double e = exp_neg(ar2, thi, tlo);
-          double v = __ldg(&a.prims[pi].coef) * e;
-          v = act ? v : 0.0;
-          t0 += v;
-          if constexpr (NC == 5) {
-            const double two_a = __ldg(&a.prims[pi].m2a) * v;
-            g += two_a;
-            h = fma(two_a, ar2, h);
+      bool folded = false;
+      if constexpr (O == Out::Planes) {
+        if (a.fold) {  // uniform: h = sum(-2 a^2 v), so that sum(-2 a v a r2) = r2 h
+          folded = true;
+          for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+            const PrimFold* F = a.fold + pi;
+            const bool act = !scr && (r2b < __ldg(&F->thr_bits));
+            if (__any_sync(kFull, act)) {
+              double v = fold_value(F, r2, r2f, fine);
+              v = act ? v : 0.0;
+              t0 += v;
+              g = fma(__ldg(&F->m2a), v, g);
+              h = fma(__ldg(&F->m2a2), v, h);
+            }
+          }
+        }
+      }
+      if (!folded) {
+        for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+          const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
+          if (__any_sync(kFull, act)) {
+            const double expo = __ldg(&a.prims[pi].expo);
+            const double ar2 = expo * r2;
+            const double e = exp_neg(ar2, thi, tlo);
+            double v = __ldg(&a.prims[pi].coef) * e;
+            v = act ? v : 0.0;
+            t0 += v;
+            if constexpr (NC == 5) {
+              const double two_a = __ldg(&a.prims[pi].m2a) * v;
+              g += two_a;
+              h = fma(two_a, ar2, h);
+            }
           }
         }
       }
       ShellVals sv;
       sv.R = t0;
       if constexpr (O == Out::Planes) {
-        // FP32 value/gradient inputs; the radial part of the Laplacian stays FP64
+        // FP32 value/gradient inputs; the radial part of the Laplacian stays FP64:
+        // Rt = 3 g - 2 sum(-2 a v a r2) + 2 l g
         const float gf = f64_to_f32(g);
         sv.Rf = f64_to_f32(t0);
         sv.t1f = gf * xf;
         sv.t2f = gf * yf;
         sv.t3f = gf * zf;
         sv.t1 = sv.t2 = sv.t3 = 0.0;
-        const double t4 = fma(-2.0, h, 3.0 * g);
-        sv.Rt = fma((double)(2 * S.l), g, t4);
+        if (folded) {
+          sv.Rt = fma(m2r2, h, (double)(3 + 2 * S.l) * g);
+        } else {
+          const double t4 = fma(-2.0, h, 3.0 * g);
+          sv.Rt = fma((double)(2 * S.l), g, t4);
+        }
       } else if constexpr (NC == 5) {
         sv.t1 = g * x;
         sv.t2 = g * y;
@@ -514,12 +586,16 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(co
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* thi = reinterpret_cast<double*>(smem_raw);
   double* tlo = thi + 32;
+  double* fine = thi + 64;  // split-BF16 planes only
   load_exp_table(a.exp_table->hi, a.exp_table->lo, thi, tlo);
+  if constexpr (O == Out::Planes)
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = a.exp_table->fine[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
   if (task >= a.task_num) return;  // warp-uniform
-  ao_task<O>(a, task, reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + 512) + warp, thi, tlo, lane);
+  ao_task<O>(a, task, reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + stage_offset<O>()) + warp, thi, tlo, fine,
+             lane);
 }
 
 // Many molecules, persistent: each warp takes the next task from a global counter until the
@@ -531,10 +607,13 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* thi = reinterpret_cast<double*>(smem_raw);
   double* tlo = thi + 32;
+  double* fine = thi + 64;  // split-BF16 planes only
   load_exp_table(mols[0].exp_table->hi, mols[0].exp_table->lo, thi, tlo);
+  if constexpr (O == Out::Planes)
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = mols[0].exp_table->fine[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + 512) + warp;
+  Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + stage_offset<O>()) + warp;
   for (;;) {
     unsigned long long t = 0;
     if (lane == 0) t = atomicAdd(counter, 1ull);
@@ -548,7 +627,7 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
       else hi = mid - 1;
     }
     const FusedArgs a = mols[lo];
-    ao_task<O>(a, task - task_begin[lo], st, thi, tlo, lane);
+    ao_task<O>(a, task - task_begin[lo], st, thi, tlo, fine, lane);
   }
 }
 
@@ -657,7 +736,7 @@ int pick_level(const AoTables& t, int64_t groups, int sms) {
 
 template <Out O>
 size_t fused_smem() {
-  return O == Out::Planes ? 512 : 512 + sizeof(Stage<ncomp<O>()>) * kWarps;
+  return O == Out::Planes ? stage_offset<O>() : stage_offset<O>() + sizeof(Stage<ncomp<O>()>) * kWarps;
 }
 
 template <Out O>
@@ -737,6 +816,7 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.chunk_num = t.level_sizes[lv];
   a.chunks = t.chunks + t.level_offsets[lv];
   a.exp_table = t.exp_table;
+  a.fold = t.fold;
   a.coord = coord;
   a.perm = perm;
   a.out = out;
@@ -854,6 +934,42 @@ __global__ void exp_check_kernel(const double* __restrict__ x, int64_t n, const 
   out[2 * i + 1] = exp(-x[i]);
 }
 }  // namespace
+
+namespace {
+// Primitive values coef * e^(-expo r2) as the split-BF16 form's AO kernel evaluates them (the
+// folded evaluation, or the FP64 form's when the tables have no folded list), zero where the
+// primitive is screened; out[i][prim_orig[k]] for packed primitive k.
+__global__ void prim_check_kernel(const PrimFold* __restrict__ fold, const PrimEntry* __restrict__ prims,
+                                  const ExpTable* __restrict__ tab, const int32_t* __restrict__ prim_orig,
+                                  const double* __restrict__ r2, int64_t n, int packed, int64_t prim_num,
+                                  double* __restrict__ out) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * packed) return;
+  const int64_t i = idx / packed;
+  const int k = (int)(idx - i * packed);
+  const double r = r2[i];
+  double v = 0.0;
+  if (fold) {
+    if (bits_of(r) < fold[k].thr_bits) v = fold_value(fold + k, r, f64_to_f32(r), tab->fine);
+  } else if (bits_of(r) < prims[k].thr_bits) {
+    v = prims[k].coef * exp_neg(prims[k].expo * r, tab->hi, tab->lo);
+  }
+  out[i * prim_num + prim_orig[k]] = v;
+}
+}  // namespace
+
+cudaError_t launch_prim_check(Ctx* ctx, const AoTables& t, const double* r2, int64_t n, int64_t prim_num,
+                              double* out) {
+  if (n <= 0 || prim_num <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double) * n * prim_num, ctx->stream);
+  if (e != cudaSuccess || t.prim_num == 0) return e;
+  const int64_t total = n * t.prim_num;
+  LaunchScope scope(ctx, "prim_check");
+  prim_check_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(t.fold, t.prims, t.exp_table,
+                                                                              t.prim_orig, r2, n, t.prim_num,
+                                                                              prim_num, out);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_exp_check(Ctx* ctx, const ExpTable* tab, const double* x, int64_t n, double* out) {
   if (n <= 0) return cudaSuccess;

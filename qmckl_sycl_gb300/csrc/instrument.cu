@@ -102,6 +102,25 @@ qmckl_exit_code_device qmckl_exp_check_device(qmckl_context_device context, cons
   return qg::finish(ctx, context, "qmckl_exp_check_device");
 }
 
+qmckl_exit_code_device qmckl_prim_value_check_device(qmckl_context_device context, const double* r2, int64_t n,
+                                                     double* out, int64_t size_max) {
+  if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
+  qg::Ctx* ctx = qg::ctx_of(context);
+  if (!ctx->ao_basis.provided)
+    return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, "qmckl_prim_value_check_device", nullptr);
+  qmckl_exit_code_device rc = qg::ensure_tables(ctx, context);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  if (!r2 || n < 0)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, "qmckl_prim_value_check_device", "bad arguments");
+  if (!out)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_4_DEVICE, "qmckl_prim_value_check_device", "NULL");
+  if (size_max < n * ctx->ao_basis.prim_num)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_5_DEVICE, "qmckl_prim_value_check_device",
+                                 "size_max < n * prim_num");
+  qg::launch_prim_check(ctx, ctx->ao_basis.tables, r2, n, ctx->ao_basis.prim_num, out);
+  return qg::finish(ctx, context, "qmckl_prim_value_check_device");
+}
+
 qmckl_exit_code_device qmckl_measure_fp64_peak_device(qmckl_context_device context, double* tflops) {
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (!tflops) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, "qmckl_measure_fp64_peak_device", "NULL");

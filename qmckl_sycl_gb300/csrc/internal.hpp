@@ -57,9 +57,26 @@ struct NucleusChunk {
 
 // 2^(j/32), j = 0..31, as hi + lo doubles (hi = the double nearest to the value): the table of
 // the AO kernel's exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989).
+// fine[j] = the double nearest to 2^(j/256), the table of the split-BF16 form's primitive values.
 struct ExpTable {
   double hi[32];
   double lo[32];
+  double fine[256];
+};
+
+// A primitive of the packed list prepared for the split-BF16 form's radials, which evaluate
+// v = coef * e^(-expo r2) as sign * 2^k * e^y with y = ln(mant) - expo r2, where
+// |coef| = mant * 2^k, mant in [1, 2): the coefficient multiply folds into the exponential.
+struct PrimFold {          // 64 bytes
+  uint64_t thr_bits;       // PrimEntry::thr_bits, or 0 (never active) for a zero coefficient
+  double na;               // -expo
+  double lnm;              // ln(mant), in [0, ln 2)
+  double m2a;              // -2 expo
+  double m2a2;             // -2 expo^2
+  float naf, lnmf;         // FP32 copies of na and lnm (the table index estimate)
+  int32_t k;               // binary exponent of |coef|
+  uint32_t sign;           // sign of coef, in bit 31
+  uint64_t pad;
 };
 
 struct AoTables {
@@ -76,6 +93,9 @@ struct AoTables {
   // chunks + level_offsets[v]; the launch picks the level that fills the GPU.
   std::vector<int32_t> level_offsets, level_sizes;
   ExpTable* exp_table = nullptr;    // device copy of the exponential's table
+  // [prim_num] packed, or null when some exponent or coefficient is outside the folded
+  // evaluation's range (then the split-BF16 form evaluates its radials like the FP64 form)
+  PrimFold* fold = nullptr;
   // grid for grouping points into spatially coherent warps: 32 cells per axis over the
   // nuclei's bounding box plus a margin (points outside are clamped to the border cells)
   double grid_origin[3] = {0, 0, 0};
@@ -86,6 +106,7 @@ struct AoTables {
   std::vector<NucleusEntry> h_nuclei;
   std::vector<ShellEntry> h_shells;
   std::vector<PrimEntry> h_prims;
+  std::vector<PrimFold> h_fold;
   std::vector<NucleusChunk> h_chunks;
   std::vector<int32_t> h_shell_orig, h_shell_nucl, h_prim_orig;
   std::vector<double> h_ao_factor;
@@ -264,6 +285,8 @@ bool ensure_raw(Ctx* ctx, void** buf, size_t* cap, size_t bytes);
 qmckl_exit_code_device ensure_tables(Ctx* ctx, qmckl_context_device c);
 const int32_t* point_order(Ctx* ctx);
 cudaError_t launch_exp_check(Ctx* ctx, const ExpTable* tab, const double* x, int64_t n, double* out);
+cudaError_t launch_prim_check(Ctx* ctx, const AoTables& t, const double* r2, int64_t n, int64_t prim_num,
+                              double* out);
 
 // Selects the context's device and creates its stream on first use.
 bool ensure_device(Ctx* ctx);
@@ -331,6 +354,7 @@ struct FusedArgs {
   const double* aof;
   const NucleusChunk* chunks;
   const ExpTable* exp_table;
+  const PrimFold* fold;     // AoTables::fold (split-BF16 planes only)
   const double* coord;      // [3][coord_ld]: x of point p at coord[p], y at coord[coord_ld + p], ...
   const int32_t* perm;      // processing order of the points, or null
   double* out;              // ao_vgl (FP64 output)

@@ -279,3 +279,51 @@ def test_point_order_does_not_change_results():
     b = run_all(s.with_points(s.coord[perm]))
     for k in a:
         assert np.array_equal(a[k][perm], b[k]), k
+
+
+def _prim_values(s, r2):
+    with Context(0) as ctx:
+        ctx.load_system(s, mo=False, points=False)
+        d = ctx.upload(r2)
+        out = ctx.buffer("prim_out", 8 * r2.size * s.prim_num)
+        ctx.call("prim_value_check", ctypes.c_void_p(d.ptr), r2.size, ctypes.c_void_p(out.ptr), r2.size * s.prim_num)
+        return ctx.download(out.ptr, (r2.size, s.prim_num))
+
+
+def _replace(s, **kw):
+    return s.__class__(**{**s.__dict__, **kw})
+
+
+@pytest.mark.parametrize("name", ["chbrclf", "medium", "signs_and_zeros", "extreme_coefficient"])
+def test_split_form_primitive_values(name, chbrclf):
+    # the split-BF16 form's AO kernel evaluates coef * e^(-expo r2) with the coefficient folded
+    # into the exponential; its values against libm, and its screening against the reference's
+    # test expo * r2 > 27.631021115928547 (bit-identical zero pattern)
+    s = chbrclf if name == "chbrclf" else config_small(3) if name != "medium" else config_medium(0, 1, 2)
+    if name == "signs_and_zeros":
+        c = s.coefficient.copy()
+        c[::7] = 0.0
+        c[1::5] *= -1.0
+        s = _replace(s, coefficient=c)
+    elif name == "extreme_coefficient":  # outside the folded range: the FP64 form's evaluation
+        c = s.coefficient.copy()
+        c[2] = 1e-300
+        s = _replace(s, coefficient=c)
+    rng = np.random.default_rng(4)
+    rmax = 27.7 / s.exponent.min()
+    r2 = np.concatenate([rng.uniform(0.0, rmax, 1000), np.exp(rng.uniform(-12, np.log(rmax), 1000)), [0.0]])
+    got = _prim_values(s, r2)
+    cn = oracle.finalize(s)["coefficient_normalized"]
+    ar2 = s.exponent[None, :] * r2[:, None]
+    screened = ar2 > 27.631021115928547
+    # long double reference (x87 extended or IEEE quad, depending on the host)
+    exact = (cn.astype(np.longdouble)[None, :] * np.exp(-(s.exponent.astype(np.longdouble)[None, :] *
+                                                            r2.astype(np.longdouble)[:, None])))
+    want = np.where(screened, 0.0, exact.astype(np.float64))
+    assert np.array_equal(got == 0.0, want == 0.0)
+    ok = np.abs(want) > 1e-290  # normal results
+    rel = (np.abs(got[ok] - exact[ok]) / np.abs(exact[ok])).astype(np.float64)
+    # the argument's rounding (|expo r2| ulp / 2) plus a few units of 1e-16
+    bound = 1.2e-16 * ar2[ok] + 6e-16
+    print("%s: max rel err %.2e, max err / bound %.2f" % (name, rel.max(), (rel / bound).max()))
+    assert (rel <= bound).all()
