@@ -154,6 +154,18 @@ struct Writer {
   int fill;                  // staged AOs
   int cap;                   // capacity of the current window
 
+  __device__ __forceinline__ void init(const FusedArgs& a, Stage<NC>* stage, int64_t p0, int ln, int nv, int64_t p,
+                                       int ao_begin) {
+    st = stage;
+    out = a.out;
+    row_len = a.row_len;
+    st->pidx[ln] = p;
+    nvalid = nv;
+    lane = ln;
+    base = ao_begin;
+    fill = 0;
+    cap = kStage - (ao_begin & (kStage - 1));
+  }
   __device__ __forceinline__ void flush() {
     __syncwarp();
     const int total = nvalid * NC * kStage;
@@ -195,53 +207,58 @@ struct Writer {
 template <>
 struct Writer<Out::Planes> {
   static constexpr int NC = 5;
-  Stage<5>* st;              // unused
-  double* out;               // unused
-  __nv_bfloat16* planes;
+  __nv_bfloat16* o;          // plane 0, AO row 0, this lane's processing slot
   int64_t plane_stride;      // kp * 5 pp
   int64_t row_len;           // 5 pp (elements per AO row)
-  int64_t pp;
-  int64_t slot;              // this lane's processing slot
-  int nvalid;
-  int lane;
+  int32_t pp;
   int base;                  // AO index of the next emit
   int fill;
-  int cap;
+  bool valid;                // the lane holds a point
 
+  __device__ __forceinline__ void init(const FusedArgs& a, Stage<5>*, int64_t p0, int ln, int nv, int64_t,
+                                       int ao_begin) {
+    o = static_cast<__nv_bfloat16*>(a.planes) + p0 + ln;
+    pp = (int32_t)a.plane_pp;
+    row_len = 5 * a.plane_pp;
+    plane_stride = a.row_len * 5 * a.plane_pp;
+    base = ao_begin;
+    fill = 0;
+    valid = ln < nv;
+  }
   __device__ __forceinline__ void flush() {
     base += fill;
     fill = 0;
   }
   __device__ __forceinline__ void emit(const double (&v)[NC]) {
-    if (lane < nvalid) {
+    if (valid) {
       // the reference's MO kernel drops an AO whose value is exactly zero from every
       // component of the point (src/qmckl_mo_sycl.cpp:40); tested on the bit pattern (+-0),
       // which keeps the FP64 pipe free
       const bool drop = (bits_of(v[0]) << 1) == 0;
-      __nv_bfloat16* o = planes + (int64_t)(base + fill) * row_len + slot;
+      __nv_bfloat16* r = o + (int64_t)(base + fill) * row_len;
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         __nv_bfloat16 h, m, l;
         split_bf16x3(c > 0 && drop ? 0.0 : v[c], h, m, l);
-        o[c * pp] = h;
-        o[plane_stride + c * pp] = m;
-        o[2 * plane_stride + c * pp] = l;
+        r[c * pp] = h;
+        r[plane_stride + c * pp] = m;
+        r[2 * plane_stride + c * pp] = l;
       }
     }
     fill += 1;
   }
   // value and gradient already in FP32, Laplacian in FP64; drop: the AO's FP64 value is zero
   __device__ __forceinline__ void emit_mixed(float v0, float gx, float gy, float gz, double lap, bool drop) {
-    if (lane < nvalid) {
-      __nv_bfloat16* o = planes + (int64_t)(base + fill) * row_len + slot;
+    if (valid) {
+      __nv_bfloat16* r = o + (int64_t)(base + fill) * row_len;
       const float vals[5] = {v0, drop ? 0.f : gx, drop ? 0.f : gy, drop ? 0.f : gz, drop ? 0.f : f64_to_f32(lap)};
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         __nv_bfloat16 h, m, l;
         split_bf16x3f(vals[c], h, m, l);
-        o[c * pp] = h;
-        o[plane_stride + c * pp] = m;
-        o[2 * plane_stride + c * pp] = l;
+        r[c * pp] = h;
+        r[plane_stride + c * pp] = m;
+        r[2 * plane_stride + c * pp] = l;
       }
     }
     fill += 1;
@@ -265,6 +282,44 @@ struct Pows {
   double X[4], Y[4], Z[4];
   float Xf[4], Yf[4], Zf[4];
 };
+
+// Powers up to L only, formed per shell: nothing of them stays live across the shell loop
+// (registers), and a nucleus without d or f shells multiplies nothing.
+template <Out O, int L>
+__device__ __forceinline__ Pows make_pows(double x, double y, double z, float xf, float yf, float zf) {
+  Pows pw;
+  pw.X[0] = pw.Y[0] = pw.Z[0] = 1.0;
+  pw.Xf[0] = pw.Yf[0] = pw.Zf[0] = 1.f;
+  if constexpr (L >= 1) {
+    pw.X[1] = x;
+    pw.Y[1] = y;
+    pw.Z[1] = z;
+    pw.Xf[1] = xf;
+    pw.Yf[1] = yf;
+    pw.Zf[1] = zf;
+  }
+  if constexpr (L >= 2) {
+    pw.X[2] = x * x;
+    pw.Y[2] = y * y;
+    pw.Z[2] = z * z;
+    if constexpr (O == Out::Planes) {
+      pw.Xf[2] = xf * xf;
+      pw.Yf[2] = yf * yf;
+      pw.Zf[2] = zf * zf;
+    }
+  }
+  if constexpr (L >= 3) {
+    pw.X[3] = pw.X[2] * x;
+    pw.Y[3] = pw.Y[2] * y;
+    pw.Z[3] = pw.Z[2] * z;
+    if constexpr (O == Out::Planes) {
+      pw.Xf[3] = pw.Xf[2] * xf;
+      pw.Yf[3] = pw.Yf[2] * yf;
+      pw.Zf[3] = pw.Zf[2] * zf;
+    }
+  }
+  return pw;
+}
 
 // One Cartesian component x^a y^b z^c (a, b, c compile-time), assembled like the
 // reference's src/qmckl_ao_sycl.cpp:371-420 and multiplied by the AO factor.
@@ -373,10 +428,11 @@ __device__ __forceinline__ void shell_fixed(Writer<O>& w, const Pows& pw, const 
   }
 }
 
-// Generic path for l >= 4 (rare): powers in local memory, same formulas.
+// Generic path for l >= 4 (rare): powers in local memory, same formulas. Inlined: a call would
+// take the address of the caller's writer and keep the hot path's writer state in local memory.
 template <Out O>
-__device__ __noinline__ void shell_generic(Writer<O>& w, double x, double y, double z, int L, const ShellVals& s,
-                                           const double* __restrict__ aof, int ao0, bool zero) {
+__device__ __forceinline__ void shell_generic(Writer<O>& w, double x, double y, double z, int L, const ShellVals& s,
+                                              const double* __restrict__ aof, int ao0, bool zero) {
   constexpr int NC = ncomp<O>();
   double X[kMaxL + 1], Y[kMaxL + 1], Z[kMaxL + 1];
   X[0] = Y[0] = Z[0] = 1.0;
@@ -417,8 +473,10 @@ __device__ __noinline__ void shell_generic(Writer<O>& w, double x, double y, dou
 }
 
 
-// One warp task: 32 points (lane = point) x one chunk of consecutive nuclei.
-template <Out O>
+// One warp task: 32 points (lane = point) x one chunk of consecutive nuclei. G: the basis has
+// shells with l >= 4 (the generic path is compiled in only then, since its local arrays and
+// extra live values cost the common kernel registers).
+template <Out O, bool G>
 __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
                                         const double* __restrict__ thi, const double* __restrict__ tlo,
                                         const double* __restrict__ fine, int lane) {
@@ -430,28 +488,11 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   const int nvalid = remaining < 32 ? (int)remaining : 32;
   const int64_t slot = p0 + (lane < nvalid ? lane : nvalid - 1);
   const int64_t p = a.perm ? (int64_t)a.perm[slot] : slot;
-  const int64_t P = a.point_num;
   const double ex = a.coord[p], ey = a.coord[a.coord_ld + p], ez = a.coord[2 * a.coord_ld + p];
 
-  Writer<O> w;
-  w.st = st;
-  w.out = a.out;
-  if constexpr (O == Out::Planes) {
-    w.planes = static_cast<__nv_bfloat16*>(a.planes);
-    w.pp = a.plane_pp;
-    w.row_len = 5 * a.plane_pp;
-    w.plane_stride = a.row_len * 5 * a.plane_pp;
-    w.slot = p0 + lane;
-  } else {
-    w.row_len = a.row_len;
-    w.st->pidx[lane] = p;
-  }
-  w.nvalid = nvalid;
-  w.lane = lane;
   const NucleusChunk cj = a.chunks[ch];
-  w.base = cj.ao_begin;
-  w.fill = 0;
-  w.cap = kStage - (cj.ao_begin & (kStage - 1));
+  Writer<O> w;
+  w.init(a, st, p0, lane, nvalid, p, cj.ao_begin);
 
   for (int n = cj.nucl_begin; n < cj.nucl_end; ++n) {
     const NucleusEntry& N = a.nuclei[n];
@@ -463,17 +504,6 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
       w.emit_zeros(N.ao_end - N.ao_begin);
       continue;
     }
-    Pows pw;
-    pw.X[0] = pw.Y[0] = pw.Z[0] = 1.0;
-    pw.X[1] = x;
-    pw.Y[1] = y;
-    pw.Z[1] = z;
-    pw.X[2] = pw.X[1] * x;
-    pw.Y[2] = pw.Y[1] * y;
-    pw.Z[2] = pw.Z[1] * z;
-    pw.X[3] = pw.X[2] * x;
-    pw.Y[3] = pw.Y[2] * y;
-    pw.Z[3] = pw.Z[2] * z;
     float xf = 0.f, yf = 0.f, zf = 0.f, r2f = 0.f;
     double m2r2 = 0.0;
     if constexpr (O == Out::Planes) {
@@ -482,16 +512,6 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
       xf = f64_to_f32(x);
       yf = f64_to_f32(y);
       zf = f64_to_f32(z);
-      pw.Xf[0] = pw.Yf[0] = pw.Zf[0] = 1.f;
-      pw.Xf[1] = xf;
-      pw.Yf[1] = yf;
-      pw.Zf[1] = zf;
-      pw.Xf[2] = xf * xf;
-      pw.Yf[2] = yf * yf;
-      pw.Zf[2] = zf * zf;
-      pw.Xf[3] = pw.Xf[2] * xf;
-      pw.Yf[3] = pw.Yf[2] * yf;
-      pw.Zf[3] = pw.Zf[2] * zf;
     }
     for (int si = N.shell_begin; si < N.shell_end; ++si) {
       const ShellEntry S = a.shells[si];
@@ -558,17 +578,19 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
         sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
       }
       switch (S.l) {
-        case 0: shell_fixed<O, 0>(w, pw, sv, a.aof, S.ao_begin, scr); break;
-        case 1: shell_fixed<O, 1>(w, pw, sv, a.aof, S.ao_begin, scr); break;
-        case 2: shell_fixed<O, 2>(w, pw, sv, a.aof, S.ao_begin, scr); break;
-        case 3: shell_fixed<O, 3>(w, pw, sv, a.aof, S.ao_begin, scr); break;
+        case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
+        case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
+        case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
+        case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
         default:
-          if constexpr (O == Out::Planes) {  // the generic path assembles in FP64
-            sv.t1 = g * x;
-            sv.t2 = g * y;
-            sv.t3 = g * z;
+          if constexpr (G) {
+            if constexpr (O == Out::Planes) {  // the generic path assembles in FP64
+              sv.t1 = g * x;
+              sv.t2 = g * y;
+              sv.t3 = g * z;
+            }
+            shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
           }
-          shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
           break;
       }
     }
@@ -580,9 +602,12 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   w.flush();
 }
 
-// One molecule: warp task = blockIdx.x * kWarps + warp.
-template <Out O>
-__global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(const FusedArgs a) {
+// One molecule. counter null: warp task = blockIdx.x * kWarps + warp. Otherwise persistent:
+// each warp takes the next task from *counter (zeroed before the launch) until none is left,
+// so that every SM gets the same share of the FP64 work whatever the grid's tail.
+template <Out O, bool G>
+__global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(const FusedArgs a,
+                                                                              unsigned long long* counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* thi = reinterpret_cast<double*>(smem_raw);
   double* tlo = thi + 32;
@@ -592,15 +617,24 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(co
     for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = a.exp_table->fine[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
-  if (task >= a.task_num) return;  // warp-uniform
-  ao_task<O>(a, task, reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + stage_offset<O>()) + warp, thi, tlo, fine,
-             lane);
+  Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + stage_offset<O>()) + warp;
+  if (!counter) {
+    const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
+    if (task < a.task_num) ao_task<O, G>(a, task, st, thi, tlo, fine, lane);  // warp-uniform
+    return;
+  }
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1ull);
+    t = __shfl_sync(kFull, t, 0);
+    if (t >= (unsigned long long)a.task_num) break;
+    ao_task<O, G>(a, (int64_t)t, st, thi, tlo, fine, lane);
+  }
 }
 
 // Many molecules, persistent: each warp takes the next task from a global counter until the
 // tasks of every molecule are done (uneven molecules balance themselves).
-template <Out O>
+template <Out O, bool G>
 __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(const FusedArgs* __restrict__ mols,
                                                                 const int64_t* __restrict__ task_begin, int nmol,
                                                                 int64_t total, unsigned long long* counter) {
@@ -626,8 +660,8 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
       if (task_begin[mid] <= task) lo = mid;
       else hi = mid - 1;
     }
-    const FusedArgs a = mols[lo];
-    ao_task<O>(a, task - task_begin[lo], st, thi, tlo, fine, lane);
+    const FusedArgs& a = mols[lo];  // fields read from global memory as needed (registers)
+    ao_task<O, G>(a, task - task_begin[lo], st, thi, tlo, fine, lane);
   }
 }
 
@@ -723,9 +757,8 @@ __global__ void cell_scatter_kernel(const int32_t* __restrict__ keys, int64_t P,
   perm[pos] = (int32_t)p;
 }
 
-// Picks the nucleus-chunk level whose task count best fills the GPU.
-int pick_level(const AoTables& t, int64_t groups, int sms) {
-  const int64_t target = (int64_t)sms * 16;  // ~16 warp tasks per SM
+// Picks the first nucleus-chunk level with at least `target` warp tasks.
+int pick_level(const AoTables& t, int64_t groups, int64_t target) {
   int best = 0;
   for (int lv = 0; lv < (int)t.level_offsets.size(); ++lv) {
     best = lv;
@@ -739,19 +772,58 @@ size_t fused_smem() {
   return O == Out::Planes ? stage_offset<O>() : stage_offset<O>() + sizeof(Stage<ncomp<O>()>) * kWarps;
 }
 
+// Resident CTAs per SM of ao_fused_kernel<O, G> (the same for every device of one build).
+template <Out O, bool G>
+int fused_per_sm() {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    const size_t smem = fused_smem<O>();
+    cudaFuncSetAttribute(ao_fused_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ao_fused_kernel<O, G>, kWarps * 32, smem) != cudaSuccess)
+      n = 1;
+    cudaGetLastError();
+    per_sm = n > 0 ? n : 1;
+  }
+  return per_sm;
+}
+
+template <Out O, bool G>
+cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
+                           double* out, __nv_bfloat16* planes, int64_t row_len, const char* name, int64_t coord_ld) {
+  const int64_t groups = (point_num + 31) / 32;
+  const size_t smem = fused_smem<O>();
+  const int per_sm = fused_per_sm<O, G>();
+  const int64_t resident_warps = (int64_t)t.sm_count * per_sm * kWarps;
+  // two or more tasks per resident warp, taken from a counter: with one task per warp the SMs
+  // that receive one CTA more than the others set the time (4 or 5 CTAs per SM on the medium
+  // workload, 16 % idle FP64 issue)
+  FusedArgs a = make_fused_args(t, pick_level(t, groups, 2 * resident_warps), coord, perm, point_num, out, planes,
+                                row_len);
+  if (coord_ld >= 0) a.coord_ld = coord_ld;
+  unsigned long long* counter = nullptr;
+  int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
+  if (a.task_num > resident_warps) {
+    if (!ctx->task_counter)
+      ctx->task_counter = static_cast<unsigned long long*>(dalloc(ctx, sizeof(unsigned long long)));
+    if (!ctx->task_counter) return cudaErrorMemoryAllocation;
+    counter = ctx->task_counter;
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return e;
+    blocks = (int64_t)t.sm_count * per_sm;
+  }
+  cudaFuncSetAttribute(ao_fused_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  LaunchScope scope(ctx, name);
+  ao_fused_kernel<O, G><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a, counter);
+  return cudaGetLastError();
+}
+
 template <Out O>
 cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
                          double* out, __nv_bfloat16* planes, int64_t row_len, const char* name, int64_t coord_ld = -1) {
   if (point_num <= 0 || t.ao_num <= 0) return cudaSuccess;
-  const int64_t groups = (point_num + 31) / 32;
-  FusedArgs a = make_fused_args(t, pick_level(t, groups, t.sm_count), coord, perm, point_num, out, planes, row_len);
-  if (coord_ld >= 0) a.coord_ld = coord_ld;
-  const int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
-  const size_t smem = fused_smem<O>();
-  cudaFuncSetAttribute(ao_fused_kernel<O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  LaunchScope scope(ctx, name);
-  ao_fused_kernel<O><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a);
-  return cudaGetLastError();
+  if (t.lmax > 3) return launch_fused_g<O, true>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
+  return launch_fused_g<O, false>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
 }
 
 __device__ __forceinline__ int morton_key(double x, double y, double z, const double* origin, double inv_cell) {
@@ -830,37 +902,52 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   return a;
 }
 
-int ao_batch_resident_ctas(bool planes) {
-  int dev = 0, sms = 152, per_sm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (planes) {
-    cudaFuncSetAttribute(ao_batch_kernel<Out::Planes>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)fused_smem<Out::Planes>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ao_batch_kernel<Out::Planes>, kWarps * 32,
-                                                  fused_smem<Out::Planes>());
-  } else {
-    cudaFuncSetAttribute(ao_batch_kernel<Out::Vgl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)fused_smem<Out::Vgl>());
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ao_batch_kernel<Out::Vgl>, kWarps * 32,
-                                                  fused_smem<Out::Vgl>());
+template <Out O, bool G>
+int batch_per_sm() {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    cudaFuncSetAttribute(ao_batch_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem<O>());
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ao_batch_kernel<O, G>, kWarps * 32, fused_smem<O>()) !=
+        cudaSuccess)
+      n = 1;
+    cudaGetLastError();
+    per_sm = n > 0 ? n : 1;
   }
-  cudaGetLastError();
-  return sms * (per_sm > 0 ? per_sm : 1);
+  return per_sm;
 }
 
-cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, const FusedArgs* mols, const int64_t* task_begin,
-                            int nmol, int64_t total, unsigned long long* counter, int grid) {
+int ao_batch_resident_ctas(bool planes, bool high_l) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaGetLastError();
+  const int per_sm = planes ? (high_l ? batch_per_sm<Out::Planes, true>() : batch_per_sm<Out::Planes, false>())
+                            : (high_l ? batch_per_sm<Out::Vgl, true>() : batch_per_sm<Out::Vgl, false>());
+  return sms * per_sm;
+}
+
+template <Out O, bool G>
+void launch_batch_g(cudaStream_t stream, const FusedArgs* mols, const int64_t* task_begin, int nmol, int64_t total,
+                    unsigned long long* counter, int grid) {
+  cudaFuncSetAttribute(ao_batch_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem<O>());
+  ao_batch_kernel<O, G><<<grid, kWarps * 32, fused_smem<O>(), stream>>>(mols, task_begin, nmol, total, counter);
+}
+
+cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, bool high_l, const FusedArgs* mols,
+                            const int64_t* task_begin, int nmol, int64_t total, unsigned long long* counter,
+                            int grid) {
   if (nmol <= 0 || total <= 0) return cudaSuccess;
-  if (grid <= 0) grid = ao_batch_resident_ctas(planes);
+  if (grid <= 0) grid = ao_batch_resident_ctas(planes, high_l);
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  if (planes)
-    ao_batch_kernel<Out::Planes><<<grid, kWarps * 32, fused_smem<Out::Planes>(), stream>>>(mols, task_begin, nmol,
-                                                                                          total, counter);
-  else
-    ao_batch_kernel<Out::Vgl><<<grid, kWarps * 32, fused_smem<Out::Vgl>(), stream>>>(mols, task_begin, nmol, total,
-                                                                                    counter);
+  if (planes) {
+    if (high_l) launch_batch_g<Out::Planes, true>(stream, mols, task_begin, nmol, total, counter, grid);
+    else launch_batch_g<Out::Planes, false>(stream, mols, task_begin, nmol, total, counter, grid);
+  } else {
+    if (high_l) launch_batch_g<Out::Vgl, true>(stream, mols, task_begin, nmol, total, counter, grid);
+    else launch_batch_g<Out::Vgl, false>(stream, mols, task_begin, nmol, total, counter, grid);
+  }
   return cudaGetLastError();
 }
 

@@ -255,6 +255,8 @@ struct qmckl_context_struct_device {
   // grow-only scratch of the adjoint (vector-Jacobian) calls
   void* vjp_buf = nullptr;
   size_t vjp_cap = 0;
+  // task counter of the persistent AO kernels (zeroed before each launch)
+  unsigned long long* task_counter = nullptr;
 
   // profiling
   bool profiling = false;
@@ -373,10 +375,12 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
                           double* out, void* planes, int64_t row_len);
 // Persistent AO kernel over the tasks of nmol molecules: mols[m]'s tasks are numbered from
 // task_begin[m] (non-decreasing, task_begin[nmol] = total); warps take tasks from *counter
-// (zeroed before the launch). planes selects the BF16-plane output. grid <= 0: resident CTAs.
-cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, const FusedArgs* mols, const int64_t* task_begin,
-                            int nmol, int64_t total, unsigned long long* counter, int grid);
-int ao_batch_resident_ctas(bool planes);
+// (zeroed before the launch). planes selects the BF16-plane output; high_l must be set when
+// some molecule has shells with l >= 4. grid <= 0: resident CTAs.
+cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, bool high_l, const FusedArgs* mols,
+                            const int64_t* task_begin, int nmol, int64_t total, unsigned long long* counter,
+                            int grid);
+int ao_batch_resident_ctas(bool planes, bool high_l);
 
 // Point order of nmol molecules at once: one Morton grid per molecule, counts [nmol][kOrderCells].
 struct OrderDesc {
