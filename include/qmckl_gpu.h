@@ -245,6 +245,27 @@ qmckl_exit_code_device qmckl_get_ao_basis_nucleus_max_ang_mom_device(qmckl_conte
 qmckl_exit_code_device qmckl_get_ao_basis_coefficient_normalized_device(qmckl_context_device context,
                                                                         double* coefficient_normalized,
                                                                         int64_t size_max);
+/* The finalize steps, run by the last setter of each basis; callable directly as in the
+ * reference (include/qmckl_gpu.hpp:651,654,796). The AO finalize ends with the per-nucleus
+ * exponent tables, as the reference's does (src/qmckl_ao_sycl.cpp:1233). */
+qmckl_exit_code_device qmckl_finalize_ao_basis_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_finalize_mo_basis_device(qmckl_context_device context);
+/* Per-nucleus exponent tables, src/qmckl_ao_sycl.cpp:855-1065 (the reference keeps them in
+ * ctx->ao_basis.{prim_num_per_nucleus, expo_per_nucleus, coef_per_nucleus}, include/
+ * qmckl_gpu.hpp:294-296; the getters below stand in for reading that struct): each nucleus'
+ * primitives sorted by exponent, equal exponents merged with their coefficients summed per
+ * shell. prim_num_per_nucleus [nucl_num] = entries per nucleus; expo_per_nucleus
+ * [nucl_num][prim_max]; coef_per_nucleus [nucl_num][shell_max][prim_max], zero where unused;
+ * prim_max = the largest primitive count of a nucleus, shell_max = the largest shell count. */
+qmckl_exit_code_device qmckl_finalize_ao_basis_hpc_device(qmckl_context_device context);
+qmckl_exit_code_device qmckl_get_ao_basis_hpc_dims_device(qmckl_context_device context, int64_t* prim_max,
+                                                          int64_t* shell_max);
+qmckl_exit_code_device qmckl_get_ao_basis_prim_num_per_nucleus_device(qmckl_context_device context,
+                                                                      int32_t* prim_num_per_nucleus, int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_expo_per_nucleus_device(qmckl_context_device context,
+                                                                  double* expo_per_nucleus, int64_t size_max);
+qmckl_exit_code_device qmckl_get_ao_basis_coef_per_nucleus_device(qmckl_context_device context,
+                                                                  double* coef_per_nucleus, int64_t size_max);
 /* Provides (lazy, date-stamped), src/qmckl_ao.cpp:47-199, src/qmckl_ao_sycl.cpp:748-849 */
 qmckl_exit_code_device qmckl_provide_ao_basis_shell_vgl_device(qmckl_context_device context);
 qmckl_exit_code_device qmckl_provide_ao_basis_ao_vgl_device(qmckl_context_device context);

@@ -66,6 +66,9 @@ def lib():
         L.oracle_mo_vgl.argtypes = [_I, _I, _I, _f64, _f64, _f64]
         L.oracle_mo_value.argtypes = [_I, _I, _I, _f64, _f64, _f64]
         L.oracle_distance.argtypes = [ctypes.c_char, ctypes.c_char, _I, _I, _f64, _I, _f64, _I, _f64, _I]
+        L.oracle_hpc_dims.argtypes = [_I, _i64, _i64, _i64, ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_int64)]
+        L.oracle_finalize_hpc.argtypes = [_I, _i64, _i64, _i64, _i64, _f64, _f64, _I, _I, _i32, _f64, _f64]
         L.oracle_vjp_mo_vgl.restype = ctypes.c_int
         L.oracle_vjp_mo_vgl.argtypes = [_I, _f64, _I, _I, _I, _i64, _i64, _i32, _i64, _i64, _f64, _f64, _f64, _f64,
                                         _f64, _I, _f64, _I, _f64, _f64, _vp, _vp, _vp]
@@ -86,6 +89,8 @@ def reference_lib():
         L.ref_run.argtypes = argt + [_vp, _vp, _vp, _vp]
         L.ref_time_mo_vgl.restype = ctypes.c_int
         L.ref_time_mo_vgl.argtypes = argt + [ctypes.c_int, _f64]
+        L.ref_hpc.restype = ctypes.c_int
+        L.ref_hpc.argtypes = argt[:16] + [_i64, _i32, _f64, _f64, _I]
         _ref = L
     return _ref
 
@@ -186,6 +191,42 @@ def finalize(s):
                          s.shell_ang_mom, s.shell_prim_index, s.shell_prim_num, s.exponent, s.coefficient,
                          s.prim_factor, s.shell_factor, npi, cn, nmax, nr)
     return dict(nucleus_prim_index=npi, coefficient_normalized=cn, nucleus_max_ang_mom=nmax, nucleus_range=nr)
+
+
+def finalize_hpc(s):
+    """Per-nucleus sorted, merged exponent tables (qmckl_finalize_ao_basis_hpc_device):
+    prim_num_per_nucleus [N] int32, expo_per_nucleus [N][prim_max], coef_per_nucleus
+    [N][shell_max][prim_max]."""
+    L = lib()
+    pm, sm = ctypes.c_int64(0), ctypes.c_int64(0)
+    L.oracle_hpc_dims(s.nucl_num, s.nucleus_index, s.nucleus_shell_num, s.shell_prim_num, ctypes.byref(pm),
+                      ctypes.byref(sm))
+    pm, sm = pm.value, sm.value
+    cn = finalize(s)["coefficient_normalized"]
+    num = np.zeros(s.nucl_num, np.int32)
+    ex = np.zeros((s.nucl_num, pm))
+    co = np.zeros((s.nucl_num, sm, pm))
+    L.oracle_finalize_hpc(s.nucl_num, s.nucleus_index, s.nucleus_shell_num, s.shell_prim_index, s.shell_prim_num,
+                          s.exponent, cn, pm, sm, num, ex, co)
+    return dict(prim_num_per_nucleus=num, expo_per_nucleus=ex, coef_per_nucleus=co)
+
+
+def reference_hpc(s):
+    """The same tables read out of the unmodified reference's context after its finalize;
+    None if the reference build is unavailable."""
+    R = reference_lib()
+    if R is None:
+        return None
+    dims = np.zeros(2, np.int64)
+    cap = max(1, s.nucl_num * s.prim_num * max(1, s.shell_num))
+    num = np.zeros(s.nucl_num, np.int32)
+    ex = np.zeros(cap)
+    co = np.zeros(cap)
+    rc = R.ref_hpc(s.nucl_num, s.charge, *_basis_args(s)[1:], dims, num, ex, co, cap)
+    assert rc == 0, rc
+    pm, sm = int(dims[0]), int(dims[1])
+    return dict(prim_num_per_nucleus=num, expo_per_nucleus=ex[:s.nucl_num * pm].reshape(s.nucl_num, pm),
+                coef_per_nucleus=co[:s.nucl_num * sm * pm].reshape(s.nucl_num, sm, pm))
 
 
 def shell_vgl(s, coord_soa=None):

@@ -92,6 +92,104 @@ void oracle_finalize_ao(int64_t nucl_num, int64_t shell_num, int64_t prim_num, c
   }
 }
 
+/*
+ * Per-nucleus exponent tables, src/qmckl_ao_sycl.cpp:855-1065 (qmckl_finalize_ao_basis_hpc_device,
+ * run by the reference at the end of qmckl_finalize_ao_basis_device, :1233):
+ *   hpc_dims(): shell_max = max nucleus_shell_num, prim_max = max over nuclei of the
+ *     nucleus' primitive count (:873-900);
+ *   for each nucleus: its primitives' exponents in shell order, sorted ascending by a
+ *     bubble sort that swaps only on a strict '<' (stable, :941-962); coef[j][i] = the
+ *     coefficient_normalized of sorted primitive i when it belongs to the nucleus' shell j,
+ *     else 0 (:964-984); consecutive equal exponents merge into one entry whose coefficient
+ *     per shell is the sum over the merged ones in sorted order (:988-1009, the entry keeps
+ *     the last merged exponent value, :1011-1013); prim_num_per_nucleus = number of entries
+ *     (1 for a nucleus without primitives, :989-1015).
+ * Outputs: prim_num_per_nucleus [nucl_num], expo_per_nucleus [nucl_num][prim_max],
+ * coef_per_nucleus [nucl_num][shell_max][prim_max] (zero where not written).
+ */
+void oracle_hpc_dims(int64_t nucl_num, const int64_t* nucleus_index, const int64_t* nucleus_shell_num,
+                     const int64_t* shell_prim_num, int64_t* prim_max, int64_t* shell_max) {
+  int64_t pm = 0, sm = 0;
+  for (int64_t n = 0; n < nucl_num; ++n) {
+    int64_t k = 0;
+    for (int64_t s = nucleus_index[n]; s < nucleus_index[n] + nucleus_shell_num[n]; ++s) k += shell_prim_num[s];
+    if (nucleus_shell_num[n] > sm) sm = nucleus_shell_num[n];
+    if (k > pm) pm = k;
+  }
+  *prim_max = pm;
+  *shell_max = sm;
+}
+
+void oracle_finalize_hpc(int64_t nucl_num, const int64_t* nucleus_index, const int64_t* nucleus_shell_num,
+                         const int64_t* shell_prim_index, const int64_t* shell_prim_num, const double* exponent,
+                         const double* coefficient_normalized, int64_t prim_max, int64_t shell_max,
+                         int32_t* prim_num_per_nucleus, double* expo_per_nucleus, double* coef_per_nucleus) {
+  for (int64_t i = 0; i < nucl_num * prim_max; ++i) expo_per_nucleus[i] = 0.0;
+  for (int64_t i = 0; i < nucl_num * shell_max * prim_max; ++i) coef_per_nucleus[i] = 0.0;
+  if (prim_max == 0) {
+    for (int64_t n = 0; n < nucl_num; ++n) prim_num_per_nucleus[n] = 0;
+    return;
+  }
+  double* ex = (double*)calloc((size_t)prim_max, sizeof(double));
+  int64_t* pos = (int64_t*)calloc((size_t)prim_max, sizeof(int64_t));  /* nucleus-local index of sorted entry */
+  int64_t* grp = (int64_t*)calloc((size_t)prim_max, sizeof(int64_t));  /* merged entry of sorted entry */
+  double* cs = (double*)calloc((size_t)(shell_max * prim_max), sizeof(double));
+  double* acc = (double*)calloc((size_t)prim_max, sizeof(double));
+  for (int64_t n = 0; n < nucl_num; ++n) {
+    const int64_t s0 = nucleus_index[n], ns = nucleus_shell_num[n];
+    int64_t k = 0;
+    for (int64_t s = s0; s < s0 + ns; ++s)
+      for (int64_t p = shell_prim_index[s]; p < shell_prim_index[s] + shell_prim_num[s]; ++p) {
+        ex[k] = exponent[p];
+        pos[k] = k;
+        ++k;
+      }
+    for (int64_t pass = 0; pass + 1 < k; ++pass)
+      for (int64_t j = 0; j + 1 < k - pass; ++j)
+        if (ex[j + 1] < ex[j]) {
+          const double te = ex[j];
+          ex[j] = ex[j + 1];
+          ex[j + 1] = te;
+          const int64_t tp = pos[j];
+          pos[j] = pos[j + 1];
+          pos[j + 1] = tp;
+        }
+    /* coefficient of sorted entry i for shell j: nonzero only if the entry is one of j's */
+    for (int64_t j = 0; j < ns; ++j) {
+      int64_t first = 0;
+      for (int64_t s = s0; s < s0 + j; ++s) first += shell_prim_num[s];
+      const int64_t last = first + shell_prim_num[s0 + j];
+      for (int64_t i = 0; i < k; ++i)
+        cs[j * prim_max + i] =
+            (pos[i] >= first && pos[i] < last) ? coefficient_normalized[shell_prim_index[s0 + j] + (pos[i] - first)]
+                                               : 0.0;
+    }
+    int64_t g = 0;
+    if (k > 0) grp[0] = 0;
+    for (int64_t i = 1; i < k; ++i) {
+      if (ex[i] != ex[i - 1]) ++g;
+      grp[i] = g;
+    }
+    for (int64_t j = 0; j < ns; ++j) {
+      for (int64_t i = 0; i < k; ++i) acc[i] = 0.0;
+      for (int64_t i = 0; i < k; ++i) acc[grp[i]] += cs[j * prim_max + i];
+      for (int64_t i = 0; i < k; ++i) cs[j * prim_max + i] = acc[i];
+    }
+    for (int64_t i = 0; i < k; ++i) ex[grp[i]] = ex[i];
+    const int64_t u = g + 1;
+    prim_num_per_nucleus[n] = (int32_t)u;
+    for (int64_t i = 0; i < u; ++i) expo_per_nucleus[n * prim_max + i] = k > 0 ? ex[i] : 0.0;
+    for (int64_t j = 0; j < ns; ++j)
+      for (int64_t i = 0; i < u; ++i)
+        coef_per_nucleus[(n * shell_max + j) * prim_max + i] = k > 0 ? cs[j * prim_max + i] : 0.0;
+  }
+  free(ex);
+  free(pos);
+  free(grp);
+  free(cs);
+  free(acc);
+}
+
 /* shell -> nucleus map, src/qmckl_ao_sycl.cpp:30-37 */
 static void shell_to_nucleus(int64_t nucl_num, const int64_t* nucleus_index, const int64_t* nucleus_shell_num,
                              int64_t shell_num, int32_t* s2n) {

@@ -135,3 +135,37 @@ extern "C" int ref_time_mo_vgl(int64_t nucl_num, const double* nucl_charge, cons
   }
   return qmckl_context_destroy_device(ctx);
 }
+
+// Per-nucleus exponent tables the reference leaves in its context after finalize
+// (qmckl_finalize_ao_basis_hpc_device, src/qmckl_ao_sycl.cpp:855-1065, run at :1233):
+// dims[0] = prim_max, dims[1] = shell_max; prim_num_per_nucleus [nucl_num],
+// expo [nucl_num][prim_max], coef [nucl_num][shell_max][prim_max] are copied out when
+// capacity (in doubles) suffices for both arrays. Returns 0 on success, -1 when too small.
+extern "C" int ref_hpc(int64_t nucl_num, const double* nucl_charge, const double* nucl_coord, int64_t shell_num,
+                       int64_t prim_num, int64_t ao_num, const int64_t* nucleus_index,
+                       const int64_t* nucleus_shell_num, const int32_t* shell_ang_mom,
+                       const int64_t* shell_prim_num, const int64_t* shell_prim_index, const double* shell_factor,
+                       const double* exponent, const double* coefficient, const double* prim_factor,
+                       const double* ao_factor, int64_t* dims, int32_t* prim_num_per_nucleus, double* expo,
+                       double* coef, int64_t capacity) {
+  sycl::queue q;
+  qmckl_context_device ctx = qmckl_context_create_device(q);
+  const double coord[3] = {0.0, 0.0, 0.0};
+  int rc = setup(ctx, nucl_num, nucl_charge, nucl_coord, shell_num, prim_num, ao_num, nucleus_index,
+                 nucleus_shell_num, shell_ang_mom, shell_prim_num, shell_prim_index, shell_factor, exponent,
+                 coefficient, prim_factor, ao_factor, 0, nullptr, 1, coord);
+  if (rc) return rc;
+  const qmckl_context_struct_device* c = reinterpret_cast<const qmckl_context_struct_device*>(ctx);
+  const int64_t pm = c->ao_basis.expo_per_nucleus.size[0];
+  const int64_t sm = c->ao_basis.coef_per_nucleus.size[1];
+  dims[0] = pm;
+  dims[1] = sm;
+  if (capacity < nucl_num * pm || capacity < nucl_num * sm * pm) {
+    qmckl_context_destroy_device(ctx);
+    return -1;
+  }
+  std::memcpy(prim_num_per_nucleus, c->ao_basis.prim_num_per_nucleus, sizeof(int32_t) * (size_t)nucl_num);
+  std::memcpy(expo, c->ao_basis.expo_per_nucleus.data, sizeof(double) * (size_t)(nucl_num * pm));
+  std::memcpy(coef, c->ao_basis.coef_per_nucleus.data, sizeof(double) * (size_t)(nucl_num * sm * pm));
+  return qmckl_context_destroy_device(ctx);
+}

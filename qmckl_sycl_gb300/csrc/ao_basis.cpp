@@ -61,6 +61,84 @@ uint64_t prim_threshold(double expo) {
 
 int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 
+// Per-nucleus exponent tables of src/qmckl_ao_sycl.cpp:855-1065: each nucleus' primitives
+// sorted by exponent (a bubble sort exchanging on a strict '<', as the reference's, so that
+// ties keep the shell order and the result is the reference's for any input), runs of equal
+// exponents merged into one entry whose per-shell coefficient is the sum of the run's
+// coefficients of that shell in sorted order (the entry keeps the run's last exponent value).
+// A nucleus without primitives reports one zero entry, like the reference.
+struct HpcTables {
+  int64_t prim_max = 0, shell_max = 0;
+  std::vector<int32_t> num;
+  std::vector<double> expo, coef;
+};
+
+HpcTables hpc_tables(int64_t N, const std::vector<int64_t>& nidx, const std::vector<int64_t>& nsh,
+                     const std::vector<int64_t>& spi, const std::vector<int64_t>& spn,
+                     const std::vector<double>& expo, const std::vector<double>& cn) {
+  HpcTables h;
+  for (int64_t n = 0; n < N; ++n) {
+    int64_t k = 0;
+    for (int64_t s = nidx[n]; s < nidx[n] + nsh[n]; ++s) k += spn[s];
+    h.prim_max = std::max(h.prim_max, k);
+    h.shell_max = std::max(h.shell_max, nsh[n]);
+  }
+  const int64_t PM = h.prim_max, SM = h.shell_max;
+  h.num.assign((size_t)N, 0);
+  h.expo.assign((size_t)(N * PM), 0.0);
+  h.coef.assign((size_t)(N * SM * PM), 0.0);
+  if (PM == 0) return h;
+  struct Entry {
+    double e;
+    int32_t shell;  // nucleus-local shell
+    int64_t prim;   // user primitive index
+  };
+  std::vector<Entry> v;
+  for (int64_t n = 0; n < N; ++n) {
+    v.clear();
+    for (int64_t j = 0; j < nsh[n]; ++j) {
+      const int64_t s = nidx[n] + j;
+      for (int64_t p = spi[s]; p < spi[s] + spn[s]; ++p) v.push_back(Entry{expo[p], (int32_t)j, p});
+    }
+    const size_t k = v.size();
+    for (size_t pass = 1; pass < k; ++pass) {
+      bool swapped = false;
+      for (size_t j = 0; j + pass < k; ++j)
+        if (v[j + 1].e < v[j].e) {
+          std::swap(v[j], v[j + 1]);
+          swapped = true;
+        }
+      if (!swapped) break;
+    }
+    double* ex = h.expo.data() + n * PM;
+    double* co = h.coef.data() + n * SM * PM;
+    int64_t u = 0;
+    for (size_t i = 0; i < k; ++i) {
+      if (i > 0 && v[i].e != v[i - 1].e) ++u;
+      ex[u] = v[i].e;
+      co[v[i].shell * PM + u] += cn[(size_t)v[i].prim];
+    }
+    h.num[(size_t)n] = (int32_t)(u + 1);
+  }
+  return h;
+}
+
+// Stores the tables in the context (device arrays), replacing earlier ones.
+qmckl_exit_code_device store_hpc(Ctx* ctx, qmckl_context_device c, const HpcTables& h, const char* fn) {
+  AoBasisData& ao = ctx->ao_basis;
+  dfree(ctx, ao.prim_num_per_nucleus);
+  dfree(ctx, ao.expo_per_nucleus);
+  dfree(ctx, ao.coef_per_nucleus);
+  ao.prim_num_per_nucleus = to_device(ctx, h.num);
+  ao.expo_per_nucleus = to_device(ctx, h.expo);
+  ao.coef_per_nucleus = to_device(ctx, h.coef);
+  ao.hpc_prim_max = h.prim_max;
+  ao.hpc_shell_max = h.shell_max;
+  if (!ao.prim_num_per_nucleus || !ao.expo_per_nucleus || !ao.coef_per_nucleus)
+    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, nullptr);
+  return QMCKL_SUCCESS_DEVICE;
+}
+
 void free_tables(Ctx* ctx, AoTables& t) {
   dfree(ctx, t.nuclei);
   dfree(ctx, t.shells);
@@ -455,6 +533,9 @@ qmckl_exit_code_device qmckl_finalize_ao_basis_device(qmckl_context_device conte
   ao.nucleus_range = to_device(ctx, nrange);
   if (!ao.nucleus_prim_index || !ao.coefficient_normalized || !ao.nucleus_max_ang_mom || !ao.nucleus_range)
     return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, fn, nullptr);
+  // the reference ends its finalize with the per-nucleus tables (src/qmckl_ao_sycl.cpp:1233)
+  rc = store_hpc(ctx, context, hpc_tables(N, nidx, nsh, spi, spn, expo, cn), fn);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
     cudaGetLastError();
     return fail(context, QMCKL_FAILURE_DEVICE, fn, "upload failed");
@@ -464,6 +545,73 @@ qmckl_exit_code_device qmckl_finalize_ao_basis_device(qmckl_context_device conte
   // Build the kernel tables now when the nuclei are placed; otherwise at first use.
   if (ao.type == 'G' && !(ctx->nucleus.uninitialized & (1 << 2))) return build_tables(ctx, context);
   return QMCKL_SUCCESS_DEVICE;
+}
+
+// src/qmckl_ao_sycl.cpp:855-1065: recomputes the per-nucleus tables of the finalized basis.
+qmckl_exit_code_device qmckl_finalize_ao_basis_hpc_device(qmckl_context_device context) {
+  const char* fn = "qmckl_finalize_ao_basis_hpc_device";
+  Ctx* ctx = checked(context);
+  if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
+  AoBasisData& ao = ctx->ao_basis;
+  if (!ao.provided || !ao.coefficient_normalized) return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, fn, nullptr);
+  const int64_t N = ctx->nucleus.num, S = ao.shell_num, K = ao.prim_num;
+  qmckl_exit_code_device rc = QMCKL_SUCCESS_DEVICE;
+  auto nidx = to_host(ctx, context, ao.nucleus_index, N, &rc);
+  auto nsh = to_host(ctx, context, ao.nucleus_shell_num, N, &rc);
+  auto spn = to_host(ctx, context, ao.shell_prim_num, S, &rc);
+  auto spi = to_host(ctx, context, ao.shell_prim_index, S, &rc);
+  auto expo = to_host(ctx, context, ao.exponent, K, &rc);
+  auto cn = to_host(ctx, context, ao.coefficient_normalized, K, &rc);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  rc = store_hpc(ctx, context, hpc_tables(N, nidx, nsh, spi, spn, expo, cn), fn);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(context, QMCKL_FAILURE_DEVICE, fn, "upload failed");
+  }
+  return QMCKL_SUCCESS_DEVICE;
+}
+
+qmckl_exit_code_device qmckl_get_ao_basis_hpc_dims_device(qmckl_context_device context, int64_t* prim_max,
+                                                          int64_t* shell_max) {
+  const char* fn = "qmckl_get_ao_basis_hpc_dims_device";
+  Ctx* ctx = checked(context);
+  if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
+  if (!ctx->ao_basis.provided || !ctx->ao_basis.prim_num_per_nucleus)
+    return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, fn, nullptr);
+  if (!prim_max) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, fn, "NULL pointer");
+  if (!shell_max) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_3_DEVICE, fn, "NULL pointer");
+  *prim_max = ctx->ao_basis.hpc_prim_max;
+  *shell_max = ctx->ao_basis.hpc_shell_max;
+  return QMCKL_SUCCESS_DEVICE;
+}
+
+qmckl_exit_code_device qmckl_get_ao_basis_prim_num_per_nucleus_device(qmckl_context_device context,
+                                                                      int32_t* prim_num_per_nucleus, int64_t size_max) {
+  Ctx* ctx = checked(context);
+  if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
+  return get_array(context, prim_num_per_nucleus, ctx->ao_basis.prim_num_per_nucleus, ctx->nucleus.num, size_max,
+                   ctx->ao_basis.provided ? 0 : kAoMaskAll, "qmckl_get_ao_basis_prim_num_per_nucleus_device",
+                   "Array too small. Expected nucl_num");
+}
+
+qmckl_exit_code_device qmckl_get_ao_basis_expo_per_nucleus_device(qmckl_context_device context,
+                                                                  double* expo_per_nucleus, int64_t size_max) {
+  Ctx* ctx = checked(context);
+  if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
+  return get_array(context, expo_per_nucleus, ctx->ao_basis.expo_per_nucleus,
+                   ctx->nucleus.num * ctx->ao_basis.hpc_prim_max, size_max, ctx->ao_basis.provided ? 0 : kAoMaskAll,
+                   "qmckl_get_ao_basis_expo_per_nucleus_device", "Array too small. Expected nucl_num * prim_max");
+}
+
+qmckl_exit_code_device qmckl_get_ao_basis_coef_per_nucleus_device(qmckl_context_device context,
+                                                                  double* coef_per_nucleus, int64_t size_max) {
+  Ctx* ctx = checked(context);
+  if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
+  return get_array(context, coef_per_nucleus, ctx->ao_basis.coef_per_nucleus,
+                   ctx->nucleus.num * ctx->ao_basis.hpc_shell_max * ctx->ao_basis.hpc_prim_max, size_max,
+                   ctx->ao_basis.provided ? 0 : kAoMaskAll, "qmckl_get_ao_basis_coef_per_nucleus_device",
+                   "Array too small. Expected nucl_num * shell_max * prim_max");
 }
 
 bool qmckl_ao_basis_provided_device(qmckl_context_device context) {

@@ -163,6 +163,11 @@ struct AoBasisData {
   double* coefficient_normalized = nullptr;
   int32_t* nucleus_max_ang_mom = nullptr;
   double* nucleus_range = nullptr;
+  // per-nucleus sorted, merged exponent tables (src/qmckl_ao_sycl.cpp:855-1065)
+  int32_t* prim_num_per_nucleus = nullptr;  // [nucl_num]
+  double* expo_per_nucleus = nullptr;       // [nucl_num][hpc_prim_max]
+  double* coef_per_nucleus = nullptr;       // [nucl_num][hpc_shell_max][hpc_prim_max]
+  int64_t hpc_prim_max = 0, hpc_shell_max = 0;
   AoTables tables;
   // caches
   double* shell_vgl = nullptr;

@@ -327,3 +327,43 @@ def test_split_form_primitive_values(name, chbrclf):
     bound = 1.2e-16 * ar2[ok] + 6e-16
     print("%s: max rel err %.2e, max err / bound %.2f" % (name, rel.max(), (rel / bound).max()))
     assert (rel <= bound).all()
+
+
+def _hpc_case(name, chbrclf):
+    if name == "chbrclf":
+        return chbrclf
+    s = config_small(2 if name == "shared_exponents" else 3)
+    if name == "shared_exponents":  # many equal exponents within nuclei and within shells
+        return _replace(s, exponent=np.round(s.exponent) + 1.0)
+    nsh, nidx = s.nucleus_shell_num.copy(), s.nucleus_index.copy()  # nucleus 1 without shells
+    nsh[0] += nsh[1]
+    nsh[1] = 0
+    nidx[1] = nidx[2]
+    return _replace(s, nucleus_shell_num=nsh, nucleus_index=nidx)
+
+
+@pytest.mark.parametrize("name", ["chbrclf", "shared_exponents", "empty_nucleus"])
+def test_finalize_hpc_tables_match_oracle(name, chbrclf):
+    # per-nucleus exponent tables (src/qmckl_ao_sycl.cpp:855-1065), bit for bit
+    s = _hpc_case(name, chbrclf)
+    ref = oracle.finalize_hpc(s)
+    N = s.nucl_num
+    with Context(0) as ctx:
+        ctx.load_system(s, mo=False, points=False)
+        for rep in range(2):  # built by the finalize, then rebuilt by the explicit call
+            pm, sm = ctypes.c_int64(0), ctypes.c_int64(0)
+            ctx.call("get_ao_basis_hpc_dims", ctypes.byref(pm), ctypes.byref(sm))
+            pm, sm = pm.value, sm.value
+            num = np.zeros(N, np.int32)
+            ex = np.zeros(N * pm)
+            co = np.zeros(N * sm * pm)
+            ctx.call("get_ao_basis_prim_num_per_nucleus", num.ctypes.data_as(ctypes.c_void_p), N)
+            ctx.call("get_ao_basis_expo_per_nucleus", ex.ctypes.data_as(ctypes.c_void_p), ex.size)
+            ctx.call("get_ao_basis_coef_per_nucleus", co.ctypes.data_as(ctypes.c_void_p), co.size)
+            assert np.array_equal(num, ref["prim_num_per_nucleus"])
+            assert np.array_equal(ex.reshape(N, pm), ref["expo_per_nucleus"])
+            assert np.array_equal(co.reshape(N, sm, pm), ref["coef_per_nucleus"])
+            ctx.call("finalize_ao_basis_hpc")
+        with pytest.raises(QmcklError) as e:
+            ctx.call("get_ao_basis_expo_per_nucleus", ex.ctypes.data_as(ctypes.c_void_p), ex.size - 1)
+        assert e.value.code == 3
