@@ -384,6 +384,63 @@ def time_batched(dist, steps, warmup, peaks, fp64_peak, molecules=64, walkers=32
     return out
 
 
+def time_shared_exponentials(dist, steps, warmup, points=40960):
+    """Shared exponentials (the per-nucleus distinct exponents of finalize_hpc) on two
+    contracted bases with `points` points around their nuclei: the CHBrClF molecule of the
+    reference's tests (5 nuclei, 297 primitives, 133 distinct exponents per nucleus, 263 AOs,
+    224 MOs) and the generally contracted synthetic basis (20 nuclei, 2060 primitives, 26
+    distinct exponents per nucleus, 1100 AOs, 300 MOs). Per form: the fused AO kernel's time
+    with sharing off, on, and as chosen automatically, and the automatic choice's points/s."""
+    from qmckl_sycl_gb300 import (PRECISION_FP64, PRECISION_SPLIT_BF16, SHARED_EXP_AUTO, SHARED_EXP_OFF,
+                                  SHARED_EXP_ON, Context)
+    from qmckl_sycl_gb300.systems import System, config_contracted
+
+    base = System.from_npz(os.path.join(ROOT, "tests", "golden", "chbrclf.npz"))
+    rng = np.random.default_rng(3)
+    nuc = base.nucl_coord.T[rng.integers(0, base.nucl_num, points)]
+    systems = [("chbrclf", base.with_points(nuc + rng.normal(scale=1.5, size=(points, 3)))),
+               ("contracted", config_contracted(0, points))]
+    out = {}
+    k = max(5, min(steps, 20))
+    for label, sy in systems:
+        ctx = Context(dist.local_rank)
+        ctx.load_system(sy)
+        entry = {"workload": "%s: %d nuclei, %d shells, %d primitives, %d AOs, %d MOs, %d points" % (
+            label, sy.nucl_num, sy.shell_num, sy.prim_num, sy.ao_num, sy.mo_num, points)}
+        for form, prec, kname, call in (
+                ("fp64", PRECISION_FP64, "ao_vgl_fused", "provide_ao_basis_ao_vgl"),
+                ("mixed", PRECISION_SPLIT_BF16, "ao_vgl_fused_bf16_planes", "provide_mo_basis_mo_vgl")):
+            ctx.set_precision(prec)
+            res = {}
+            for mlabel, mode in (("off", SHARED_EXP_OFF), ("on", SHARED_EXP_ON), ("auto", SHARED_EXP_AUTO)):
+                ctx.set_shared_exponentials(mode)
+                for _ in range(warmup):
+                    ctx.touch()
+                    ctx.call(call)
+                ctx.synchronize()
+                ctx.set_profiling(True)
+                ctx.reset_kernel_stats()
+                ctx.call("timer_start")
+                for _ in range(k):
+                    ctx.touch()
+                    ctx.call(call)
+                ms = ctypes.c_double(0)
+                ctx.call("timer_stop", ctypes.byref(ms))
+                st = ctx.kernel_stats()
+                ctx.set_profiling(False)
+                n, tot = st.get(kname, (0, 0.0))
+                res[mlabel] = (tot / n if n else None, ms.value / k)
+                if mlabel == "auto":
+                    res["auto_active"] = ctx.shared_exponentials()
+            entry[form] = {"ao_kernel": kname, "ao_ms_off": res["off"][0], "ao_ms_on": res["on"][0],
+                           "ao_ms_auto": res["auto"][0], "auto_shares": res["auto_active"],
+                           "ao_speedup_on": res["off"][0] / res["on"][0] if res["off"][0] and res["on"][0] else None,
+                           "step_ms_auto": res["auto"][1], "points_per_s_auto": points / (res["auto"][1] * 1e-3)}
+        ctx.close()
+        out[label] = entry
+    return out
+
+
 def time_adjoint(dist, steps, warmup, fp64_peak):
     """The adjoint form on its workload (8 nuclei, ~200 AOs, 64 MOs, 2048 points): one step =
     new points + qmckl_vjp_mo_vgl_device for all three gradients (coefficients, exponents,
@@ -541,6 +598,7 @@ def main():
         cpu = {"value": v, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample}
 
     adj = time_adjoint(dist, args.steps, args.warmup, fp64_peak.value)
+    shared = time_shared_exponentials(dist, args.steps, args.warmup)
     bt = None
     if not args.no_batched:
         bt = time_batched(dist, args.steps, args.warmup, peaks, fp64_peak.value, args.batch_molecules,
@@ -567,6 +625,7 @@ def main():
         line["mixed_vs_fp64_error"] = acc
         line["mixed_over_fp64"] = results["mixed"]["value"] / results["fp64"]["value"]
     line["adjoint"] = adj
+    line["shared_exponentials"] = shared
     if bt:
         line["batched"] = bt
     print(json.dumps(line), flush=True)

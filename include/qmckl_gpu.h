@@ -319,6 +319,22 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_value_inplace_device(qmckl_context_
 qmckl_exit_code_device qmckl_set_precision_mode_device(qmckl_context_device context, int32_t mode);
 qmckl_exit_code_device qmckl_get_precision_mode_device(qmckl_context_device context, int32_t* mode);
 
+/* Shared exponentials of the fused AO kernels. Contracted bases repeat exponents among the
+ * shells of a nucleus (CHBrClF: 297 primitives, 133 distinct exponents per nucleus); with
+ * sharing on, the kernels evaluate each distinct exponential once per point and nucleus and
+ * the shells' primitives multiply it by their coefficients. AUTO (default) shares for the
+ * FP64 AO outputs when the distinct exponents carry at most half of the primitives' active
+ * volume (sum of a^-1.5; generally contracted bases), and not for the split-BF16 planes; ON
+ * shares for both; at most 64 distinct exponents per nucleus are supported (off beyond). The
+ * FP64 results are bit-identical either way; in the split-BF16 mode the radials are rounded
+ * differently (well inside the mode's tolerance). The get function reports whether the current
+ * basis shares in the current precision mode (needs a finalized AO basis). */
+#define QMCKL_SHARED_EXP_AUTO_DEVICE (-1)
+#define QMCKL_SHARED_EXP_OFF_DEVICE 0
+#define QMCKL_SHARED_EXP_ON_DEVICE 1
+qmckl_exit_code_device qmckl_set_ao_shared_exponentials_device(qmckl_context_device context, int32_t mode);
+qmckl_exit_code_device qmckl_get_ao_shared_exponentials_device(qmckl_context_device context, int32_t* active);
+
 /* Asynchronous mode: when on, calls return after enqueueing their work on the
  * context's stream (no host wait). Off by default (the reference waits on every call). */
 qmckl_exit_code_device qmckl_set_async_device(qmckl_context_device context, int32_t async);

@@ -16,6 +16,7 @@ SUCCESS = 0
 INVALID_ARG_2, INVALID_ARG_3, INVALID_ARG_4 = 2, 3, 4
 FAILURE, INVALID_CONTEXT, ALLOCATION_FAILED, NOT_PROVIDED, ALREADY_SET = 101, 103, 104, 106, 108
 PRECISION_FP64, PRECISION_SPLIT_BF16 = 0, 1
+SHARED_EXP_AUTO, SHARED_EXP_OFF, SHARED_EXP_ON = -1, 0, 1
 
 
 class QmcklError(RuntimeError):
@@ -214,6 +215,14 @@ class Context:
 
     def set_precision(self, mode):
         self.call("set_precision_mode", int(mode))
+
+    def set_shared_exponentials(self, mode):
+        self.call("set_ao_shared_exponentials", int(mode))
+
+    def shared_exponentials(self):
+        v = ctypes.c_int32(0)
+        self.call("get_ao_shared_exponentials", ctypes.byref(v))
+        return bool(v.value)
 
     def vjp_mo_vgl(self, w, want=("coef", "expo", "coord"), prim_num=None):
         """Gradients of sum(w * mo_vgl) (w: [P][5][M] numpy): dict with 'coef' [M][A],

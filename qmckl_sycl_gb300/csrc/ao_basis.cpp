@@ -150,8 +150,12 @@ void free_tables(Ctx* ctx, AoTables& t) {
   dfree(ctx, t.chunks);
   dfree(ctx, t.exp_table);
   dfree(ctx, t.fold);
+  dfree(ctx, t.ent);
   t.exp_table = nullptr;
   t.fold = nullptr;
+  t.ent = nullptr;
+  t.ent_cap = 0;
+  t.ent_forced = false;
   t.nuclei = nullptr;
   t.shells = nullptr;
   t.prims = nullptr;
@@ -217,6 +221,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   t.h_shells.clear();
   t.h_prims.clear();
   t.h_fold.clear();
+  t.h_ent.clear();
   t.h_chunks.clear();
   t.h_shell_orig.clear();
   t.h_prim_orig.clear();
@@ -249,6 +254,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
         pe.expo = expo[p];
         pe.coef = cn[p];
         pe.m2a = -2.0 * expo[p];
+        pe.m2a2 = -2.0 * (expo[p] * expo[p]);
         pe.thr_bits = prim_threshold(expo[p]);
         t.h_prims.push_back(pe);
         t.h_prim_orig.push_back((int32_t)p);
@@ -343,6 +349,57 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
     t.sm_count = sms;
   cudaGetLastError();
+  // distinct exponents per nucleus. Worth sharing when they save most of the exponentials that
+  // points actually evaluate: a primitive is active within r2 <= 27.6 / a, a volume ~ a^-1.5,
+  // so the measure is sum over distinct exponents of a^-1.5 / sum over primitives of a^-1.5
+  // (CHBrClF 0.75: its repeated exponents are mostly steep; generally contracted bases ~0.25);
+  // every exponent positive and finite
+  {
+    bool ok = true;
+    int64_t total = 0;
+    int32_t cap = 0;
+    double w_all = 0.0, w_ent = 0.0;
+    for (const PrimEntry& pe : t.h_prims)
+      if (!(pe.expo > 0.0) || !std::isfinite(pe.expo)) ok = false;
+    std::vector<double> ex;
+    for (size_t n = 0; ok && n < t.h_nuclei.size(); ++n) {
+      NucleusEntry& e = t.h_nuclei[n];
+      const int32_t p0 = e.shell_end > e.shell_begin ? t.h_shells[(size_t)e.shell_begin].prim_begin : 0;
+      const int32_t p1 = e.shell_end > e.shell_begin ? t.h_shells[(size_t)e.shell_end - 1].prim_end : 0;
+      ex.clear();
+      for (int32_t p = p0; p < p1; ++p) ex.push_back(t.h_prims[(size_t)p].expo);
+      std::sort(ex.begin(), ex.end());
+      ex.erase(std::unique(ex.begin(), ex.end()), ex.end());
+      e.ent_begin = (int32_t)t.h_ent.size();
+      e.ent_num = (int32_t)ex.size();
+      for (int32_t p = p0; p < p1; ++p) w_all += std::pow(t.h_prims[(size_t)p].expo, -1.5);
+      for (double a : ex) {
+        w_ent += std::pow(a, -1.5);
+        PrimFold f{};
+        f.thr_bits = prim_threshold(a);
+        f.na = -a;
+        f.m2a = -2.0 * a;
+        f.m2a2 = -2.0 * (a * a);
+        f.naf = (float)f.na;
+        t.h_ent.push_back(f);
+      }
+      for (int32_t p = p0; p < p1; ++p)
+        t.h_prims[(size_t)p].ent =
+            (int32_t)(std::lower_bound(ex.begin(), ex.end(), t.h_prims[(size_t)p].expo) - ex.begin());
+      total += (int64_t)ex.size();
+      cap = std::max(cap, (int32_t)ex.size());
+    }
+    const int32_t mode = ctx->shared_exp;
+    const bool worth = w_all > 0.0 && w_ent <= 0.5 * w_all;
+    if (ok && cap > 0 && cap <= 64 && mode != QMCKL_SHARED_EXP_OFF_DEVICE &&
+        (worth || mode == QMCKL_SHARED_EXP_ON_DEVICE)) {
+      t.ent_cap = cap;
+      t.ent_forced = mode == QMCKL_SHARED_EXP_ON_DEVICE;
+    } else {
+      t.h_ent.clear();
+      t.ent_cap = 0;
+    }
+  }
   t.nuclei = to_device(ctx, t.h_nuclei);
   t.shells = to_device(ctx, t.h_shells);
   t.prims = to_device(ctx, t.h_prims);
@@ -360,6 +417,13 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   }
   t.chunks = to_device(ctx, t.h_chunks);
   t.exp_table = to_device(ctx, et);
+  if (t.ent_cap > 0) {
+    t.ent = to_device(ctx, t.h_ent);
+    if (!t.ent) {
+      free_tables(ctx, t);
+      return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "kernel tables");
+    }
+  }
   if (fold_ok && !t.h_fold.empty()) {
     t.fold = to_device(ctx, t.h_fold);
     if (!t.fold) {
@@ -612,6 +676,32 @@ qmckl_exit_code_device qmckl_get_ao_basis_coef_per_nucleus_device(qmckl_context_
                    ctx->nucleus.num * ctx->ao_basis.hpc_shell_max * ctx->ao_basis.hpc_prim_max, size_max,
                    ctx->ao_basis.provided ? 0 : kAoMaskAll, "qmckl_get_ao_basis_coef_per_nucleus_device",
                    "Array too small. Expected nucl_num * shell_max * prim_max");
+}
+
+qmckl_exit_code_device qmckl_set_ao_shared_exponentials_device(qmckl_context_device context, int32_t mode) {
+  const char* fn = "qmckl_set_ao_shared_exponentials_device";
+  Ctx* ctx = checked(context);
+  if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
+  if (mode != QMCKL_SHARED_EXP_AUTO_DEVICE && mode != QMCKL_SHARED_EXP_OFF_DEVICE && mode != QMCKL_SHARED_EXP_ON_DEVICE)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, fn, "mode must be AUTO (-1), OFF (0) or ON (1)");
+  if (ctx->shared_exp != mode) {
+    ctx->shared_exp = mode;
+    ctx->ao_basis.tables.valid = false;  // rebuilt at the next evaluation
+    invalidate_caches(ctx);
+  }
+  return QMCKL_SUCCESS_DEVICE;
+}
+
+qmckl_exit_code_device qmckl_get_ao_shared_exponentials_device(qmckl_context_device context, int32_t* active) {
+  const char* fn = "qmckl_get_ao_shared_exponentials_device";
+  Ctx* ctx = checked(context);
+  if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
+  if (!active) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, fn, "NULL pointer");
+  if (!ctx->ao_basis.provided) return qmckl_failwith_device(context, QMCKL_NOT_PROVIDED_DEVICE, fn, nullptr);
+  qmckl_exit_code_device rc = ensure_tables(ctx, context);
+  if (rc != QMCKL_SUCCESS_DEVICE) return rc;
+  *active = ao_shared_exponentials(ctx->ao_basis.tables, ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE) ? 1 : 0;
+  return QMCKL_SUCCESS_DEVICE;
 }
 
 bool qmckl_ao_basis_provided_device(qmckl_context_device context) {

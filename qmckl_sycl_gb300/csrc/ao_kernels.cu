@@ -476,10 +476,10 @@ __device__ __forceinline__ void shell_generic(Writer<O>& w, double x, double y, 
 // One warp task: 32 points (lane = point) x one chunk of consecutive nuclei. G: the basis has
 // shells with l >= 4 (the generic path is compiled in only then, since its local arrays and
 // extra live values cost the common kernel registers).
-template <Out O, bool G>
+template <Out O, bool G, bool B>
 __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
                                         const double* __restrict__ thi, const double* __restrict__ tlo,
-                                        const double* __restrict__ fine, int lane) {
+                                        const double* __restrict__ fine, double* __restrict__ ebuf, int lane) {
   constexpr int NC = ncomp<O>();
   const int64_t group = task / a.chunk_num;
   const int ch = (int)(task - group * a.chunk_num);
@@ -513,12 +513,55 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
       yf = f64_to_f32(y);
       zf = f64_to_f32(z);
     }
+    // Shared exponentials (B): each distinct exponent of the nucleus once per lane, kept in
+    // this lane's column of the warp's buffer; the shells' primitives then read them. The
+    // FP64 outputs evaluate coef * e^(-expo r2) with the same operations as the per-primitive
+    // loop (bit-identical results).
+    bool shared_e = false;
+    if constexpr (B) {
+      if (a.ent) {
+        shared_e = true;
+        for (int u = 0; u < N.ent_num; ++u) {
+          const PrimFold* E = a.ent + N.ent_begin + u;
+          const bool act = !scr && (r2b < __ldg(&E->thr_bits));
+          if (__any_sync(kFull, act)) {
+            double e;
+            if constexpr (O == Out::Planes) e = fold_value(E, r2, r2f, fine);
+            else e = exp_neg((-__ldg(&E->na)) * r2, thi, tlo);
+            ebuf[u * 32 + lane] = act ? e : 0.0;
+          }
+        }
+      }
+    }
     for (int si = N.shell_begin; si < N.shell_end; ++si) {
       const ShellEntry S = a.shells[si];
       double t0 = 0.0, g = 0.0, h = 0.0;
       bool folded = false;
+      if constexpr (B) {
+        if (shared_e) {
+          folded = O == Out::Planes;
+          for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+            const PrimEntry* P = a.prims + pi;
+            const bool act = !scr && (r2b < __ldg(&P->thr_bits));
+            if (__any_sync(kFull, act)) {
+              double v = __ldg(&P->coef) * ebuf[__ldg(&P->ent) * 32 + lane];
+              v = act ? v : 0.0;
+              t0 += v;
+              if constexpr (O == Out::Planes) {
+                g = fma(__ldg(&P->m2a), v, g);
+                h = fma(__ldg(&P->m2a2), v, h);
+              } else if constexpr (NC == 5) {
+                const double ar2 = __ldg(&P->expo) * r2;
+                const double two_a = __ldg(&P->m2a) * v;
+                g += two_a;
+                h = fma(two_a, ar2, h);
+              }
+            }
+          }
+        }
+      }
       if constexpr (O == Out::Planes) {
-        if (a.fold) {  // uniform: h = sum(-2 a^2 v), so that sum(-2 a v a r2) = r2 h
+        if (!shared_e && a.fold) {  // uniform: h = sum(-2 a^2 v), so that sum(-2 a v a r2) = r2 h
           folded = true;
           for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
             const PrimFold* F = a.fold + pi;
@@ -533,7 +576,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
           }
         }
       }
-      if (!folded) {
+      if (!folded && !shared_e) {
         for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
           const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
           if (__any_sync(kFull, act)) {
@@ -602,25 +645,46 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   w.flush();
 }
 
+// Dynamic shared memory of the fused kernels: tables, staging buffers (ao_vgl / ao_value), then
+// with shared exponentials one column of ent_cap doubles per lane.
+template <Out O>
+__host__ __device__ constexpr size_t fused_smem(int ent_cap = 0) {
+  const size_t base = O == Out::Planes ? stage_offset<O>() : stage_offset<O>() + sizeof(Stage<ncomp<O>()>) * kWarps;
+  return base + (size_t)kWarps * 32 * sizeof(double) * (size_t)(ent_cap > 0 ? ent_cap : 0);
+}
+
+// Per-CTA setup shared by the kernels: the exponential's tables into shared memory, and this
+// warp's staging buffer and exponential buffer.
+template <Out O>
+struct CtaSmem {
+  double *thi, *tlo, *fine, *ebuf;
+  Stage<ncomp<O>()>* st;
+  __device__ __forceinline__ CtaSmem(unsigned char* raw, const ExpTable* tab, int ent_cap, int warp) {
+    thi = reinterpret_cast<double*>(raw);
+    tlo = thi + 32;
+    fine = thi + 64;  // split-BF16 planes only
+    load_exp_table(tab->hi, tab->lo, thi, tlo);
+    if constexpr (O == Out::Planes)
+      for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = tab->fine[i];
+    st = reinterpret_cast<Stage<ncomp<O>()>*>(raw + stage_offset<O>()) + warp;
+    ebuf = reinterpret_cast<double*>(raw + fused_smem<O>(0)) + (size_t)warp * 32 * (ent_cap > 0 ? ent_cap : 0);
+  }
+};
+
 // One molecule. counter null: warp task = blockIdx.x * kWarps + warp. Otherwise persistent:
 // each warp takes the next task from *counter (zeroed before the launch) until none is left,
 // so that every SM gets the same share of the FP64 work whatever the grid's tail.
-template <Out O, bool G>
+// G: shells with l >= 4 exist; B: shared exponentials (a.ent non-null).
+template <Out O, bool G, bool B>
 __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(const FusedArgs a,
                                                                               unsigned long long* counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* thi = reinterpret_cast<double*>(smem_raw);
-  double* tlo = thi + 32;
-  double* fine = thi + 64;  // split-BF16 planes only
-  load_exp_table(a.exp_table->hi, a.exp_table->lo, thi, tlo);
-  if constexpr (O == Out::Planes)
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = a.exp_table->fine[i];
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + stage_offset<O>()) + warp;
+  const CtaSmem<O> sm(smem_raw, a.exp_table, B ? a.ent_cap : 0, warp);
+  __syncthreads();
   if (!counter) {
     const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
-    if (task < a.task_num) ao_task<O, G>(a, task, st, thi, tlo, fine, lane);  // warp-uniform
+    if (task < a.task_num) ao_task<O, G, B>(a, task, sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);  // warp-uniform
     return;
   }
   for (;;) {
@@ -628,26 +692,22 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(co
     if (lane == 0) t = atomicAdd(counter, 1ull);
     t = __shfl_sync(kFull, t, 0);
     if (t >= (unsigned long long)a.task_num) break;
-    ao_task<O, G>(a, (int64_t)t, st, thi, tlo, fine, lane);
+    ao_task<O, G, B>(a, (int64_t)t, sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);
   }
 }
 
 // Many molecules, persistent: each warp takes the next task from a global counter until the
-// tasks of every molecule are done (uneven molecules balance themselves).
-template <Out O, bool G>
+// tasks of every molecule are done (uneven molecules balance themselves). ent_cap: the largest
+// AoTables::ent_cap of the molecules with shared exponentials (B).
+template <Out O, bool G, bool B>
 __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(const FusedArgs* __restrict__ mols,
                                                                 const int64_t* __restrict__ task_begin, int nmol,
-                                                                int64_t total, unsigned long long* counter) {
+                                                                int64_t total, unsigned long long* counter,
+                                                                int ent_cap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* thi = reinterpret_cast<double*>(smem_raw);
-  double* tlo = thi + 32;
-  double* fine = thi + 64;  // split-BF16 planes only
-  load_exp_table(mols[0].exp_table->hi, mols[0].exp_table->lo, thi, tlo);
-  if constexpr (O == Out::Planes)
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = mols[0].exp_table->fine[i];
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Stage<ncomp<O>()>* st = reinterpret_cast<Stage<ncomp<O>()>*>(smem_raw + stage_offset<O>()) + warp;
+  const CtaSmem<O> sm(smem_raw, mols[0].exp_table, B ? ent_cap : 0, warp);
+  __syncthreads();
   for (;;) {
     unsigned long long t = 0;
     if (lane == 0) t = atomicAdd(counter, 1ull);
@@ -661,7 +721,7 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
       else hi = mid - 1;
     }
     const FusedArgs& a = mols[lo];  // fields read from global memory as needed (registers)
-    ao_task<O, G>(a, task - task_begin[lo], st, thi, tlo, fine, lane);
+    ao_task<O, G, B>(a, task - task_begin[lo], sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);
   }
 }
 
@@ -767,33 +827,29 @@ int pick_level(const AoTables& t, int64_t groups, int64_t target) {
   return best;
 }
 
-template <Out O>
-size_t fused_smem() {
-  return O == Out::Planes ? stage_offset<O>() : stage_offset<O>() + sizeof(Stage<ncomp<O>()>) * kWarps;
+
+// Resident CTAs per SM of a kernel with `smem` bytes of dynamic shared memory.
+template <class K>
+int resident_per_sm(K kernel, size_t smem) {
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kWarps * 32, smem) != cudaSuccess) n = 1;
+  cudaGetLastError();
+  return n > 0 ? n : 1;
 }
 
-// Resident CTAs per SM of ao_fused_kernel<O, G> (the same for every device of one build).
-template <Out O, bool G>
-int fused_per_sm() {
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    const size_t smem = fused_smem<O>();
-    cudaFuncSetAttribute(ao_fused_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ao_fused_kernel<O, G>, kWarps * 32, smem) != cudaSuccess)
-      n = 1;
-    cudaGetLastError();
-    per_sm = n > 0 ? n : 1;
-  }
-  return per_sm;
-}
-
-template <Out O, bool G>
+template <Out O, bool G, bool B>
 cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
                            double* out, __nv_bfloat16* planes, int64_t row_len, const char* name, int64_t coord_ld) {
   const int64_t groups = (point_num + 31) / 32;
-  const size_t smem = fused_smem<O>();
-  const int per_sm = fused_per_sm<O, G>();
+  const size_t smem = fused_smem<O>(B ? t.ent_cap : 0);
+  static size_t cached_smem = 0;
+  static int cached_per_sm = 0;
+  if (cached_smem != smem || cached_per_sm == 0) {
+    cached_per_sm = resident_per_sm(ao_fused_kernel<O, G, B>, smem);
+    cached_smem = smem;
+  }
+  const int per_sm = cached_per_sm;
   const int64_t resident_warps = (int64_t)t.sm_count * per_sm * kWarps;
   // two or more tasks per resident warp, taken from a counter: with one task per warp the SMs
   // that receive one CTA more than the others set the time (4 or 5 CTAs per SM on the medium
@@ -801,6 +857,8 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
   FusedArgs a = make_fused_args(t, pick_level(t, groups, 2 * resident_warps), coord, perm, point_num, out, planes,
                                 row_len);
   if (coord_ld >= 0) a.coord_ld = coord_ld;
+  a.ent = B ? t.ent : nullptr;
+  a.ent_cap = B ? t.ent_cap : 0;
   unsigned long long* counter = nullptr;
   int64_t blocks = (a.task_num + kWarps - 1) / kWarps;
   if (a.task_num > resident_warps) {
@@ -812,18 +870,32 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
     if (e != cudaSuccess) return e;
     blocks = (int64_t)t.sm_count * per_sm;
   }
-  cudaFuncSetAttribute(ao_fused_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(ao_fused_kernel<O, G, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   LaunchScope scope(ctx, name);
-  ao_fused_kernel<O, G><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a, counter);
+  ao_fused_kernel<O, G, B><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a, counter);
   return cudaGetLastError();
+}
+
+// Without an explicit request, sharing serves the FP64 outputs only (the tables exist only
+// when the basis passes the activity-weighted test at build time). Measured on 40960 points:
+// generally contracted basis (26 distinct exponents for 103 primitives per nucleus) ao_vgl
+// 3.19 -> 2.60 ms although the buffer halves the resident CTAs, but the split-BF16 planes
+// 1.44 -> 1.50 ms (their folded primitive costs 10 FP64 instructions against 18, so less is
+// saved); CHBrClF (repeats mostly among steep, mostly screened primitives) ao_vgl 0.58 -> 0.72.
+template <Out O>
+bool share_by_default() {
+  return O != Out::Planes;
 }
 
 template <Out O>
 cudaError_t launch_fused(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
                          double* out, __nv_bfloat16* planes, int64_t row_len, const char* name, int64_t coord_ld = -1) {
   if (point_num <= 0 || t.ao_num <= 0) return cudaSuccess;
-  if (t.lmax > 3) return launch_fused_g<O, true>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
-  return launch_fused_g<O, false>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
+  const bool g = t.lmax > 3, b = t.ent != nullptr && (t.ent_forced || share_by_default<O>());
+  if (g && b) return launch_fused_g<O, true, true>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
+  if (g) return launch_fused_g<O, true, false>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
+  if (b) return launch_fused_g<O, false, true>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
+  return launch_fused_g<O, false, false>(ctx, t, coord, perm, point_num, out, planes, row_len, name, coord_ld);
 }
 
 __device__ __forceinline__ int morton_key(double x, double y, double z, const double* origin, double inv_cell) {
@@ -877,6 +949,11 @@ __global__ void batch_scatter_kernel(const OrderDesc* __restrict__ desc, const i
 
 int ao_level_count(const AoTables& t) { return (int)t.level_offsets.size(); }
 
+bool ao_shared_exponentials(const AoTables& t, bool planes) {
+  if (!t.ent) return false;
+  return t.ent_forced || (planes ? share_by_default<Out::Planes>() : share_by_default<Out::Vgl>());
+}
+
 FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
                           double* out, void* planes, int64_t row_len) {
   const int lv = level < 0 ? 0 : (level >= (int)t.level_offsets.size() ? (int)t.level_offsets.size() - 1 : level);
@@ -889,6 +966,9 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.chunks = t.chunks + t.level_offsets[lv];
   a.exp_table = t.exp_table;
   a.fold = t.fold;
+  const bool share = ao_shared_exponentials(t, planes != nullptr);
+  a.ent = share ? t.ent : nullptr;
+  a.ent_cap = share ? t.ent_cap : 0;
   a.coord = coord;
   a.perm = perm;
   a.out = out;
@@ -902,52 +982,52 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   return a;
 }
 
-template <Out O, bool G>
-int batch_per_sm() {
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    cudaFuncSetAttribute(ao_batch_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem<O>());
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ao_batch_kernel<O, G>, kWarps * 32, fused_smem<O>()) !=
-        cudaSuccess)
-      n = 1;
-    cudaGetLastError();
-    per_sm = n > 0 ? n : 1;
-  }
-  return per_sm;
+template <Out O, bool G, bool B>
+int batch_per_sm(int ent_cap) {
+  return resident_per_sm(ao_batch_kernel<O, G, B>, fused_smem<O>(B ? ent_cap : 0));
 }
 
-int ao_batch_resident_ctas(bool planes, bool high_l) {
+template <Out O>
+int batch_per_sm_of(bool high_l, int ent_cap) {
+  if (high_l) return ent_cap > 0 ? batch_per_sm<O, true, true>(ent_cap) : batch_per_sm<O, true, false>(0);
+  return ent_cap > 0 ? batch_per_sm<O, false, true>(ent_cap) : batch_per_sm<O, false, false>(0);
+}
+
+int ao_batch_resident_ctas(bool planes, bool high_l, int ent_cap) {
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaGetLastError();
-  const int per_sm = planes ? (high_l ? batch_per_sm<Out::Planes, true>() : batch_per_sm<Out::Planes, false>())
-                            : (high_l ? batch_per_sm<Out::Vgl, true>() : batch_per_sm<Out::Vgl, false>());
+  const int per_sm = planes ? batch_per_sm_of<Out::Planes>(high_l, ent_cap) : batch_per_sm_of<Out::Vgl>(high_l, ent_cap);
   return sms * per_sm;
 }
 
-template <Out O, bool G>
+template <Out O, bool G, bool B>
 void launch_batch_g(cudaStream_t stream, const FusedArgs* mols, const int64_t* task_begin, int nmol, int64_t total,
-                    unsigned long long* counter, int grid) {
-  cudaFuncSetAttribute(ao_batch_kernel<O, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem<O>());
-  ao_batch_kernel<O, G><<<grid, kWarps * 32, fused_smem<O>(), stream>>>(mols, task_begin, nmol, total, counter);
+                    unsigned long long* counter, int grid, int ent_cap) {
+  const size_t smem = fused_smem<O>(B ? ent_cap : 0);
+  cudaFuncSetAttribute(ao_batch_kernel<O, G, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  ao_batch_kernel<O, G, B><<<grid, kWarps * 32, smem, stream>>>(mols, task_begin, nmol, total, counter, ent_cap);
 }
 
-cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, bool high_l, const FusedArgs* mols,
+template <Out O>
+void launch_batch_of(cudaStream_t stream, bool high_l, int ent_cap, const FusedArgs* mols, const int64_t* task_begin,
+                     int nmol, int64_t total, unsigned long long* counter, int grid) {
+  if (high_l && ent_cap > 0) launch_batch_g<O, true, true>(stream, mols, task_begin, nmol, total, counter, grid, ent_cap);
+  else if (high_l) launch_batch_g<O, true, false>(stream, mols, task_begin, nmol, total, counter, grid, 0);
+  else if (ent_cap > 0) launch_batch_g<O, false, true>(stream, mols, task_begin, nmol, total, counter, grid, ent_cap);
+  else launch_batch_g<O, false, false>(stream, mols, task_begin, nmol, total, counter, grid, 0);
+}
+
+cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, bool high_l, int ent_cap, const FusedArgs* mols,
                             const int64_t* task_begin, int nmol, int64_t total, unsigned long long* counter,
                             int grid) {
   if (nmol <= 0 || total <= 0) return cudaSuccess;
-  if (grid <= 0) grid = ao_batch_resident_ctas(planes, high_l);
+  if (grid <= 0) grid = ao_batch_resident_ctas(planes, high_l, ent_cap);
   cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  if (planes) {
-    if (high_l) launch_batch_g<Out::Planes, true>(stream, mols, task_begin, nmol, total, counter, grid);
-    else launch_batch_g<Out::Planes, false>(stream, mols, task_begin, nmol, total, counter, grid);
-  } else {
-    if (high_l) launch_batch_g<Out::Vgl, true>(stream, mols, task_begin, nmol, total, counter, grid);
-    else launch_batch_g<Out::Vgl, false>(stream, mols, task_begin, nmol, total, counter, grid);
-  }
+  if (planes) launch_batch_of<Out::Planes>(stream, high_l, ent_cap, mols, task_begin, nmol, total, counter, grid);
+  else launch_batch_of<Out::Vgl>(stream, high_l, ent_cap, mols, task_begin, nmol, total, counter, grid);
   return cudaGetLastError();
 }
 

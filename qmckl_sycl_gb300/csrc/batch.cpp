@@ -55,6 +55,7 @@ struct qmckl_batch_struct_device {
   int64_t ao_tasks = 0, total_points = 0;
   int gemm_tiles = 0, ao_grid = 0;
   bool high_l = false;  // some member has shells with l >= 4
+  int ent_cap = 0;       // largest shared-exponential buffer of a member (0: none shares)
   std::vector<uintptr_t> sig;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -251,13 +252,16 @@ qmckl_exit_code_device build_descriptors(Batch* b, const std::vector<Member>& ms
   std::vector<FusedArgs> args(n);
   std::vector<double> task_cost(n);
   b->high_l = false;
+  b->ent_cap = 0;
   for (int i = 0; i < n; ++i) {
     const Member& e = ms[i];
     const AoTables& t = e.ctx->ao_basis.tables;
     if (t.lmax > 3) b->high_l = true;
+
     const int level = b->tune.v[0] < 0 ? 0 : std::min(b->tune.v[0], ao_level_count(t) - 1);
     args[i] = make_fused_args(t, level, e.ctx->point.coord, e.ctx->ao_basis.point_perm, e.P, e.ao_vgl, e.planes,
                               split ? e.kp : e.A);
+    if (args[i].ent) b->ent_cap = std::max(b->ent_cap, args[i].ent_cap);
     task_cost[i] = ((double)t.prim_num + 0.5 * (double)t.ao_num) / (double)args[i].chunk_num;
   }
   std::vector<int> ao_order(n);
@@ -364,7 +368,7 @@ qmckl_exit_code_device build_descriptors(Batch* b, const std::vector<Member>& ms
   b->total_points = point_begin[n];
   b->ao_tasks = ao_begin[n];
   b->gemm_tiles = (int)tiles;
-  b->ao_grid = ao_batch_resident_ctas(split, b->high_l);
+  b->ao_grid = ao_batch_resident_ctas(split, b->high_l, b->ent_cap);
   return QMCKL_SUCCESS_DEVICE;
 }
 
@@ -379,7 +383,7 @@ cudaError_t stage_order(Batch* b, cudaStream_t s) {
 }
 
 cudaError_t stage_ao(Batch* b, cudaStream_t s) {
-  return launch_ao_batch(s, b->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE, b->high_l,
+  return launch_ao_batch(s, b->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE, b->high_l, b->ent_cap,
                          at<FusedArgs>(b, b->off_ao_args),
                          at<int64_t>(b, b->off_ao_begin), b->n_ao, b->ao_tasks,
                          at<unsigned long long>(b, b->off_counter64), b->ao_grid);

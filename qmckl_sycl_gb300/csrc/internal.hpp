@@ -33,7 +33,9 @@ struct NucleusEntry {      // 64 bytes
                            // like their bit patterns), the reference's test at ao_sycl.cpp:53
   int32_t shell_begin, shell_end;  // range in the packed shell list
   int32_t ao_begin, ao_end;        // AO columns of this nucleus
-  int32_t lmax, pad;
+  int32_t lmax;
+  int32_t ent_begin, ent_num;      // distinct exponents of the nucleus in AoTables::ent
+  int32_t pad;
 };
 struct ShellEntry {        // 16 bytes
   int32_t prim_begin, prim_end;  // range in the packed primitive list
@@ -41,12 +43,15 @@ struct ShellEntry {        // 16 bytes
   int16_t l;
   int16_t orig;            // unused (the original index lives in shell_orig)
 };
-struct PrimEntry {         // 32 bytes
+struct PrimEntry {         // 48 bytes
   double expo;
   double coef;             // coefficient_normalized = coefficient * prim_factor * shell_factor
   double m2a;              // -2 * expo (exact)
+  double m2a2;             // -2 * expo^2
   uint64_t thr_bits;       // bits of the smallest r2 with fl(expo * r2) > cutoff: the primitive
                            // is skipped iff bits(r2) >= thr_bits (ao_sycl.cpp:72-75)
+  int32_t ent;             // index of its exponent among the nucleus' distinct exponents
+  int32_t pad;
 };
 
 // A contiguous group of nuclei processed by one warp task.
@@ -96,6 +101,12 @@ struct AoTables {
   // [prim_num] packed, or null when some exponent or coefficient is outside the folded
   // evaluation's range (then the split-BF16 form evaluates its radials like the FP64 form)
   PrimFold* fold = nullptr;
+  // Distinct exponents per nucleus (NucleusEntry::ent_begin/ent_num), as PrimFold entries with
+  // coefficient 1, when the basis repeats exponents within nuclei enough for the kernels to
+  // evaluate each exponential once per nucleus and share it between shells (null otherwise).
+  PrimFold* ent = nullptr;
+  int32_t ent_cap = 0;              // largest distinct-exponent count of a nucleus
+  bool ent_forced = false;          // sharing requested explicitly (else: FP64 outputs only)
   // grid for grouping points into spatially coherent warps: 32 cells per axis over the
   // nuclei's bounding box plus a margin (points outside are clamped to the border cells)
   double grid_origin[3] = {0, 0, 0};
@@ -106,7 +117,7 @@ struct AoTables {
   std::vector<NucleusEntry> h_nuclei;
   std::vector<ShellEntry> h_shells;
   std::vector<PrimEntry> h_prims;
-  std::vector<PrimFold> h_fold;
+  std::vector<PrimFold> h_fold, h_ent;
   std::vector<NucleusChunk> h_chunks;
   std::vector<int32_t> h_shell_orig, h_shell_nucl, h_prim_orig;
   std::vector<double> h_ao_factor;
@@ -237,6 +248,7 @@ struct qmckl_context_struct_device {
   cudaStream_t copy_stream = nullptr;  // device-to-host copies overlapped with compute
   bool async = false;
   int32_t precision = QMCKL_PRECISION_FP64_DEVICE;
+  int32_t shared_exp = QMCKL_SHARED_EXP_AUTO_DEVICE;  // shared exponentials of the AO kernels
 
   std::recursive_mutex mutex;
   int lock_count = 0;
@@ -362,6 +374,8 @@ struct FusedArgs {
   const NucleusChunk* chunks;
   const ExpTable* exp_table;
   const PrimFold* fold;     // AoTables::fold (split-BF16 planes only)
+  const PrimFold* ent;      // AoTables::ent, or null
+  int ent_cap;              // AoTables::ent_cap
   const double* coord;      // [3][coord_ld]: x of point p at coord[p], y at coord[coord_ld + p], ...
   const int32_t* perm;      // processing order of the points, or null
   double* out;              // ao_vgl (FP64 output)
@@ -376,16 +390,21 @@ struct FusedArgs {
 };
 // Number of nucleus-chunk levels of the tables (level v has about 2^v chunks).
 int ao_level_count(const AoTables& t);
+// Whether the fused AO kernel for ao_vgl (planes false) or the BF16 planes (true) shares the
+// exponentials of t: t.ent exists and either sharing was requested explicitly or the output
+// is FP64.
+bool ao_shared_exponentials(const AoTables& t, bool planes);
 FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
                           double* out, void* planes, int64_t row_len);
 // Persistent AO kernel over the tasks of nmol molecules: mols[m]'s tasks are numbered from
 // task_begin[m] (non-decreasing, task_begin[nmol] = total); warps take tasks from *counter
 // (zeroed before the launch). planes selects the BF16-plane output; high_l must be set when
-// some molecule has shells with l >= 4. grid <= 0: resident CTAs.
-cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, bool high_l, const FusedArgs* mols,
+// some molecule has shells with l >= 4; ent_cap is the largest AoTables::ent_cap of the
+// molecules with shared exponentials (0: none). grid <= 0: resident CTAs.
+cudaError_t launch_ao_batch(cudaStream_t stream, bool planes, bool high_l, int ent_cap, const FusedArgs* mols,
                             const int64_t* task_begin, int nmol, int64_t total, unsigned long long* counter,
                             int grid);
-int ao_batch_resident_ctas(bool planes, bool high_l);
+int ao_batch_resident_ctas(bool planes, bool high_l, int ent_cap);
 
 // Point order of nmol molecules at once: one Morton grid per molecule, counts [nmol][kOrderCells].
 struct OrderDesc {

@@ -19,6 +19,12 @@ shapes and value distributions the benchmark configurations name):
   batched 64 molecules, 5-60 nuclei, 100-1500 AOs, 20-400 MOs, small-config generators,
           32 walkers x 2*nuclei electrons each
   adjoint 8 nuclei, ~200 AOs, 64 MOs, 2048 points
+  contracted  generally contracted basis (the form of ANO and correlation-consistent sets):
+          per nucleus one set of primitive exponents per angular momentum (10 s, 8 p, 5 d,
+          3 f, log-uniform [0.05, 50]) shared by all shells of that angular momentum
+          (5 s, 4 p, 3 d, 2 f shells, coefficients U(-1, 1)); 20 nuclei in a 12-bohr cube
+          (1100 AOs, 2060 primitives, 26 distinct exponents per nucleus), 300 MOs, points
+          ~ N(nucleus, 1.5^2)
 """
 from dataclasses import dataclass, field
 
@@ -157,3 +163,43 @@ def config_batched(seed=0, molecules=64, walkers=32):
         out.append(make_system(None, N, 8, cube, S, SPD_WEIGHTS, 5, (0.05, 50.0), M, P, 1.5,
                                name="batched[%d]" % m, rng=rng))
     return out
+
+
+def config_contracted(seed=0, point_num=40960, nucl_num=20, mo_num=300):
+    """Generally contracted synthetic basis: shells of one angular momentum on a nucleus share
+    that nucleus' primitive exponents and differ in their coefficients."""
+    rng = np.random.default_rng(seed)
+    N = int(nucl_num)
+    charge = rng.integers(1, 11, size=N).astype(np.float64)
+    nucl_coord = rng.uniform(0.0, 12.0, size=(3, N))
+    layout = ((0, 5, 10), (1, 4, 8), (2, 3, 5), (3, 2, 3))  # (l, shells, primitives per shell)
+    ang, nprim, expo, coef, nsh = [], [], [], [], []
+    for n in range(N):
+        cnt = 0
+        for l, shells, k in layout:
+            ex = np.sort(np.exp(rng.uniform(np.log(0.05), np.log(50.0), size=k)))[::-1]
+            for _ in range(shells):
+                ang.append(l)
+                nprim.append(k)
+                expo.append(ex)
+                coef.append(rng.uniform(-1.0, 1.0, size=k))
+                cnt += 1
+        nsh.append(cnt)
+    ang = np.asarray(ang, np.int32)
+    nprim = np.asarray(nprim, np.int64)
+    S, K = len(ang), int(nprim.sum())
+    nucleus_shell_num = np.asarray(nsh, np.int64)
+    nucleus_index = np.concatenate([[0], np.cumsum(nucleus_shell_num)[:-1]]).astype(np.int64)
+    shell_prim_index = np.concatenate([[0], np.cumsum(nprim)[:-1]]).astype(np.int64)
+    A = int(sum(ncart(int(l)) for l in ang))
+    M = min(int(mo_num), A)
+    mo_coef = rng.normal(0.0, 1.0 / np.sqrt(A), size=(M, A))
+    centers = rng.integers(0, N, size=int(point_num))
+    coord = nucl_coord[:, centers].T + rng.normal(0.0, 1.5, size=(int(point_num), 3))
+    return System(
+        nucl_num=N, charge=charge, nucl_coord=np.ascontiguousarray(nucl_coord), shell_num=S, prim_num=K, ao_num=A,
+        nucleus_index=nucleus_index, nucleus_shell_num=nucleus_shell_num, shell_ang_mom=ang, shell_prim_num=nprim,
+        shell_prim_index=shell_prim_index, shell_factor=np.ones(S), exponent=np.concatenate(expo),
+        coefficient=np.concatenate(coef), prim_factor=np.ones(K), ao_factor=np.ones(A), mo_num=M,
+        mo_coef=np.ascontiguousarray(mo_coef), coord=np.ascontiguousarray(coord), name="contracted",
+        meta=dict(seed=seed, layout=layout))
