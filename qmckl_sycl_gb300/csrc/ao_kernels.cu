@@ -99,6 +99,16 @@ __device__ __forceinline__ void split_bf16x3(double a, __nv_bfloat16& h, __nv_bf
   split_bf16x3f(f64_to_f32(a), h, m, l);
 }
 
+// c ? v : +0.0 on the bit pattern (an integer AND instead of a select of doubles).
+__device__ __forceinline__ double keep_if(bool c, double v) {
+  return __longlong_as_double(__double_as_longlong(v) & -(long long)c);
+}
+
+// 2l and 3 + 2l of the radial Laplacian term as doubles, by l (no integer-to-FP64 conversion
+// per shell).
+__constant__ double kTwoL[kMaxL + 1] = {0, 2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 38};
+__constant__ double kThreePlusTwoL[kMaxL + 1] = {3, 5, 7, 9, 11, 13, 15, 17, 19, 21, 23, 25, 27, 29, 31, 33, 35, 37, 39, 41};
+
 // -n as a double, exactly, with integer instructions only (n = 0 gives 0).
 __device__ __forceinline__ double neg_int_to_double(int n) {
   const unsigned u = n < 0 ? 0u - (unsigned)n : (unsigned)n;
@@ -106,7 +116,7 @@ __device__ __forceinline__ double neg_int_to_double(int n) {
   // the mantissa's leading bit carries into the exponent field: (1022 + msb) + 1
   const unsigned long long b = ((unsigned long long)(1022 + msb) << 52) + ((unsigned long long)u << (52 - msb));
   const unsigned long long sg = n > 0 ? 0x8000000000000000ull : 0ull;
-  return u == 0 ? 0.0 : __longlong_as_double((long long)(b | sg));
+  return __longlong_as_double((long long)((b | sg) & (u == 0 ? 0ull : ~0ull)));
 }
 
 constexpr float kInvL256f = 369.32993f;                  // 256 / ln 2 (only picks the table index)
@@ -528,7 +538,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
             double e;
             if constexpr (O == Out::Planes) e = fold_value(E, r2, r2f, fine);
             else e = exp_neg((-__ldg(&E->na)) * r2, thi, tlo);
-            ebuf[u * 32 + lane] = act ? e : 0.0;
+            ebuf[u * 32 + lane] = keep_if(act, e);
           }
         }
       }
@@ -545,7 +555,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
             const bool act = !scr && (r2b < __ldg(&P->thr_bits));
             if (__any_sync(kFull, act)) {
               double v = __ldg(&P->coef) * ebuf[__ldg(&P->ent) * 32 + lane];
-              v = act ? v : 0.0;
+              v = keep_if(act, v);
               t0 += v;
               if constexpr (O == Out::Planes) {
                 g = fma(__ldg(&P->m2a), v, g);
@@ -568,7 +578,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
             const bool act = !scr && (r2b < __ldg(&F->thr_bits));
             if (__any_sync(kFull, act)) {
               double v = fold_value(F, r2, r2f, fine);
-              v = act ? v : 0.0;
+              v = keep_if(act, v);
               t0 += v;
               g = fma(__ldg(&F->m2a), v, g);
               h = fma(__ldg(&F->m2a2), v, h);
@@ -584,7 +594,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
             const double ar2 = expo * r2;
             const double e = exp_neg(ar2, thi, tlo);
             double v = __ldg(&a.prims[pi].coef) * e;
-            v = act ? v : 0.0;
+            v = keep_if(act, v);
             t0 += v;
             if constexpr (NC == 5) {
               const double two_a = __ldg(&a.prims[pi].m2a) * v;
@@ -606,17 +616,17 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
         sv.t3f = gf * zf;
         sv.t1 = sv.t2 = sv.t3 = 0.0;
         if (folded) {
-          sv.Rt = fma(m2r2, h, (double)(3 + 2 * S.l) * g);
+          sv.Rt = fma(m2r2, h, kThreePlusTwoL[S.l] * g);
         } else {
           const double t4 = fma(-2.0, h, 3.0 * g);
-          sv.Rt = fma((double)(2 * S.l), g, t4);
+          sv.Rt = fma(kTwoL[S.l], g, t4);
         }
       } else if constexpr (NC == 5) {
         sv.t1 = g * x;
         sv.t2 = g * y;
         sv.t3 = g * z;
         const double t4 = fma(-2.0, h, 3.0 * g);
-        sv.Rt = fma((double)(2 * S.l), g, t4);
+        sv.Rt = fma(kTwoL[S.l], g, t4);
       } else {
         sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
       }
