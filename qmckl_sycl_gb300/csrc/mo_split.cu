@@ -44,8 +44,15 @@ namespace {
 constexpr int kBM = 128;        // rows per tile (UMMA M)
 constexpr int kBK = 64;         // K per stage: 64 BF16 = 128 bytes = one swizzle row
 constexpr int kStages = 2;
-constexpr int kMaxN = 96;       // columns per tile: 5 * N <= 512 TMEM columns
-constexpr int kThreads = 320;   // 10 warps: TMA, MMA, 4 fold warps, 4 store warps
+constexpr int kMaxN = 96;       // columns per tile (the fold warps hold 2 x kMaxN sums per row)
+constexpr int kThreads = 384;   // 12 warps = 3 warpgroups: {TMA, MMA, 2 idle}, 4 fold warps, 4 store warps
+constexpr int kBufs = 3;         // main-product TMEM buffers: the MMAs run up to two fold groups ahead
+constexpr int kFold = 2;         // K blocks (of 64) per main-product block sum folded into the two-sum
+// registers per thread after setmaxnreg: warpgroup 0 (TMA, MMA), 1 (fold), 2 (store); launched
+// with 168 per thread: 384 x 168 = 64512 >= 128 x (112 + 248 + 88) = 57344
+constexpr int kRegsIssue = 112;
+constexpr int kRegsFold = 248;
+constexpr int kRegsStore = 88;
 constexpr uint32_t kPlaneA = kBM * kBK * 2;  // 16 KB per A plane and stage
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
 
@@ -301,9 +308,100 @@ __device__ __forceinline__ TileRef tile_ref(const SplitJob* __restrict__ jobs, i
   return t;
 }
 
-// Tensor-memory columns: [0,N) corrections, [N,2N) and [2N,3N) main product ping-pong
-// buffers (one 64-wide K block each), [3N,4N) and [4N,5N) the running FP32 two-sum (hi, lo)
-// of the main product, folded in by the epilogue warps after every K block.
+template <int R>
+__device__ __forceinline__ void reg_dec() {
+  asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(R));
+}
+__device__ __forceinline__ void reg_inc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(kRegsFold)); }
+
+// What the fold warps of a CTA share across tiles.
+struct FoldCtx {
+  uint32_t lb;                       // TMEM address of this warp's 32 lanes, column 0
+  float* stg;                        // this warp's 32 rows of the output staging buffer
+  uint64_t *accf, *acce, *tmem_free, *out_ready, *out_free;
+  volatile int* abort_flag;
+  int* error;
+  int lane;
+};
+
+// The fold warps' work on one tile of N columns (one row per thread): after every kFold K
+// blocks, the main product's FP32 block sum from TMEM is added into a running two-sum (hi, lo) held in
+// registers (a TMEM round trip of hi and lo per K block would add 4N column accesses to the N
+// of the main buffer, and tensor-memory traffic slows the MMAs that share it: 20 % of the
+// kernel's time on the medium workload); at the end hi + (lo + corrections) goes to the staging
+// buffer. it: the running fold-group index (advanced), tl: the CTA's tile count. Returns false
+// when a wait gave up.
+__device__ __forceinline__ bool fold_tile(const FoldCtx& f, int N, int kblocks, uint32_t& it, uint32_t tl) {
+  float rhi[kMaxN], rlo[kMaxN];
+  const int groups = (kblocks + kFold - 1) / kFold;
+  for (int kb = 0; kb < groups; ++kb, ++it) {
+    const uint32_t b = it % kBufs, use = it / kBufs;
+    // warp-uniform decision: the tcgen05.ld below are .sync.aligned
+    if (!__all_sync(0xffffffffu, wait_or_abort(&f.accf[b], use & 1u, f.abort_flag))) {
+      if (f.lane == 0) set_abort(f.abort_flag, f.error, 4);
+      return false;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+    for (int c0 = 0; c0 < kMaxN; c0 += 16) {
+      if (c0 < N) {
+        uint32_t rv[16];
+        tmem_ld16_async(f.lb + (1 + b) * (uint32_t)N + (uint32_t)c0, rv);
+        tmem_wait_ld(rv);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          if (kb == 0) {
+            rhi[c0 + q] = __uint_as_float(rv[q]);
+            rlo[c0 + q] = 0.f;
+          } else {
+            float s2, e2;
+            two_sum(rhi[c0 + q], __uint_as_float(rv[q]), s2, e2);
+            rhi[c0 + q] = s2;
+            rlo[c0 + q] += e2;
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncwarp();
+    if (f.lane == 0) mbar_arrive(&f.acce[b]);
+  }
+  // The last accf phase covered every MMA of the tile, corrections included: read the
+  // corrections out into the staging buffer with the two-sum (once the store warps have written
+  // out the previous tile), then release tensor memory to the next tile and the staging buffer
+  // to the store warps.
+  if (tl > 0 && !__all_sync(0xffffffffu, wait_or_abort(f.out_free, (tl - 1) & 1u, f.abort_flag))) {
+    if (f.lane == 0) set_abort(f.abort_flag, f.error, 7);
+    return false;
+  }
+  const int pitch = kMaxN + 1;  // odd pitch spreads the rows over the banks
+#pragma unroll
+  for (int c0 = 0; c0 < kMaxN; c0 += 16) {
+    if (c0 < N) {
+      uint32_t rc[16];
+      tmem_ld16_async(f.lb + (uint32_t)c0, rc);
+      tmem_wait_ld(rc);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) {
+        float s2, e2;
+        two_sum(rhi[c0 + q], __uint_as_float(rc[q]), s2, e2);
+        // hi + (lo + e) rounded once to FP32 (2^-24 relative)
+        f.stg[f.lane * pitch + c0 + q] = s2 + (rlo[c0 + q] + e2);
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncwarp();
+  if (f.lane == 0) {
+    mbar_arrive(f.tmem_free);
+    mbar_arrive(f.out_ready);
+  }
+  return true;
+}
+
+// Tensor-memory columns: [0,N) corrections, then kBufs main-product buffers of N columns (one
+// 64-wide K block each, rotating), folded into the fold warps' register two-sum after every K
+// block.
 //
 // Persistent and continuous: CTA b processes tiles b, b + gridDim.x, ... of the launch (tiles
 // of one job are ordered column tile fastest, so CTAs running at the same time share A rows in
@@ -320,9 +418,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   float* out_stage = (float*)(base + kStages * max_stage);
   uint64_t* full = (uint64_t*)(base + kStages * max_stage + kOutStage);
   uint64_t* empty = full + kStages;
-  uint64_t* accf = empty + kStages;  // [2] main buffer filled (MMA -> epilogue)
-  uint64_t* acce = accf + 2;         // [2] main buffer folded (epilogue -> MMA)
-  uint64_t* tmem_free = acce + 2;    // accumulators of the last tile read out (epilogue -> MMA)
+  uint64_t* accf = empty + kStages;  // [kBufs] main buffer filled (MMA -> epilogue)
+  uint64_t* acce = accf + kBufs;     // [kBufs] main buffer folded (epilogue -> MMA)
+  uint64_t* tmem_free = acce + kBufs;  // accumulators of the last tile read out (epilogue -> MMA)
   uint64_t* out_ready = tmem_free + 1;  // staging buffer filled (fold warps -> store warps)
   uint64_t* out_free = out_ready + 1;   // staging buffer written out (store warps -> fold warps)
   uint64_t* mma_done = out_free + 1;
@@ -342,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(&full[s2], 1);
       mbar_init(&empty[s2], 1);
     }
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kBufs; ++b) {
       mbar_init(&accf[b], 1);
       mbar_init(&acce[b], 4);
     }
@@ -356,8 +454,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-
+  // Registers move from the producer/MMA and store warpgroups to the fold warpgroup; each role
+  // adjusts its warpgroup's allocation on entry (all four warps of a warpgroup do the same).
   if (warp == 0) {
+    reg_dec<kRegsIssue>();
     if (lane == 0) {
       // ---------------- TMA producer
       uint32_t it = 0;  // running K-block index over the CTA's tiles
@@ -394,9 +494,10 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (uint32_t q = first; q < it; ++q) mbar_wait(&full[q % kStages], (q / kStages) & 1u);
     }
   } else if (warp == 1) {
+    reg_dec<kRegsIssue>();
     if (lane == 0) {
       // ---------------- MMA issuer
-      uint32_t it = 0, tl = 0;
+      uint32_t it = 0, tl = 0, gi = 0;  // running K block, tile and fold-group indices
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x, ++tl) {
         const TileRef tr = tile_ref(jobs, njobs, tile);
@@ -415,8 +516,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
-          const uint32_t s2 = it % kStages, ph = (it / kStages) & 1u, b = it & 1u, use = it >> 1;
-          if (use > 0 && !wait_or_abort(&acce[b], (use - 1) & 1u, abort_flag)) {
+          const uint32_t s2 = it % kStages, ph = (it / kStages) & 1u, b = gi % kBufs, use = gi / kBufs;
+          const bool first = kb % kFold == 0, last = kb % kFold == kFold - 1 || kb == job.kblocks - 1;
+          if (first && use > 0 && !wait_or_abort(&acce[b], (use - 1) & 1u, abort_flag)) {
             set_abort(abort_flag, error, 2);
             ok = false;
             break;
@@ -438,16 +540,22 @@ __global__ void __launch_bounds__(kThreads, 1)
             const uint64_t a = da + kk * ka, bb = db + kk * 2u;
             // (A plane, B plane): main (0,0); corrections (0,1) (1,0) (0,2) (1,1) (2,0)
             umma_six(main_acc, tmem, a, bb, a, bb + pb, a + pa, bb, a, bb + 2 * pb, a + pa, bb + pb, a + 2 * pa, bb, idesc,
-                     kk > 0 ? 1u : 0u, (kb | kk) != 0 ? 1u : 0u);
+                     (first && kk == 0) ? 0u : 1u, (kb | kk) != 0 ? 1u : 0u);
           }
           umma_commit(&empty[s2]);  // frees the stage once these MMAs have read it
-          umma_commit(&accf[b]);    // main buffer b holds this block's product
+          if (last) {
+            umma_commit(&accf[b]);  // main buffer b holds this group's product
+            ++gi;
+          }
         }
       }
       umma_commit(mma_done);  // every MMA issued has completed
       if (!mbar_wait(mma_done, 0)) set_abort(abort_flag, error, 5);
     }
-  } else if (warp < 6) {
+  } else if (warp < 4) {
+    reg_dec<kRegsIssue>();  // warps 2 and 3: no role (they complete warpgroup 0)
+  } else if (warp < 8) {
+    reg_inc();
     // ---------------- fold warps: warp w owns TMEM lanes 32*(w % 4) .. +31 (one row per thread)
     const int quarter = warp & 3;
     const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
@@ -457,87 +565,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x, ++tl) {
       const TileRef tr = tile_ref(jobs, njobs, tile);
       const SplitJob& job = *tr.job;
-      const int N = job.n_tile;
-      const uint32_t hi_col = 3 * N, lo_col = 4 * N;
-      for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
-        const uint32_t b = it & 1u, use = it >> 1;
-        // warp-uniform decision: the tcgen05.ld/st below are .sync.aligned
-        if (!__all_sync(0xffffffffu, wait_or_abort(&accf[b], use & 1u, abort_flag))) {
-          if (lane == 0) set_abort(abort_flag, error, 4);
-          ok = false;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // one TMEM round trip per 16 columns: the main block and the running (hi, lo) together
-        for (int c0 = 0; c0 < N; c0 += 16) {
-          uint32_t rv[16], rh[16], rl[16];
-          float hi[16], lo[16];
-          tmem_ld16_async(lb + (1 + b) * (uint32_t)N + (uint32_t)c0, rv);
-          if (kb > 0) {
-            tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
-            tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
-          }
-          tmem_wait_ld(rv);
-          if (kb == 0) {
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              hi[q] = __uint_as_float(rv[q]);
-              lo[q] = 0.f;
-            }
-          } else {
-            tmem_wait_ld(rh);
-            tmem_wait_ld(rl);
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              float s2, e2;
-              two_sum(__uint_as_float(rh[q]), __uint_as_float(rv[q]), s2, e2);
-              hi[q] = s2;
-              lo[q] = __uint_as_float(rl[q]) + e2;
-            }
-          }
-          tmem_st16(lb + hi_col + (uint32_t)c0, hi);
-          tmem_st16(lb + lo_col + (uint32_t)c0, lo);
-        }
-        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&acce[b]);
-      }
-      if (!ok) break;
-      // The last accf phase covered every MMA of the tile, corrections included: read the
-      // accumulators out into the staging buffer (once the store warps have written out the
-      // previous tile), then release tensor memory to the next tile and the staging buffer to the
-      // store warps.
-      if (tl > 0 && !__all_sync(0xffffffffu, wait_or_abort(out_free, (tl - 1) & 1u, abort_flag))) {
-        if (lane == 0) set_abort(abort_flag, error, 7);
-        break;
-      }
-      const int pitch = kMaxN + 1;  // odd pitch spreads the rows over the banks
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        uint32_t rc[16], rh[16], rl[16];
-        tmem_ld16_async(lb + (uint32_t)c0, rc);
-        tmem_ld16_async(lb + hi_col + (uint32_t)c0, rh);
-        tmem_ld16_async(lb + lo_col + (uint32_t)c0, rl);
-        tmem_wait_ld(rc);
-        tmem_wait_ld(rh);
-        tmem_wait_ld(rl);
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          float s2, e2;
-          two_sum(__uint_as_float(rh[q]), __uint_as_float(rc[q]), s2, e2);
-          // hi + (lo + e) rounded once to FP32 (2^-24 relative); an FP64 add here would cost the
-          // FP64 pipe ~10k cycles per tile
-          stg[lane * pitch + c0 + q] = s2 + (__uint_as_float(rl[q]) + e2);
-        }
-      }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) {
-        mbar_arrive(tmem_free);
-        mbar_arrive(out_ready);
-      }
+      FoldCtx f{lb, stg, accf, acce, tmem_free, out_ready, out_free, abort_flag, error, lane};
+      ok = fold_tile(f, job.n_tile, job.kblocks, it, tl);
     }
   } else {
+    reg_dec<kRegsStore>();
     // ---------------- store warps: write each tile's staged rows as contiguous row segments
     // (one thread per row would write 32 scattered 8-byte pieces per instruction)
     const int quarter = warp & 3;
