@@ -790,32 +790,51 @@ __global__ void morton_key_kernel(const double* __restrict__ coord, int64_t ld, 
 }
 
 // In-place exclusive prefix sum of kOrderCells counters per CTA of 1024 threads (CTA b scans
-// the counters of molecule b).
+// the counters of molecule b): each thread scans 32 consecutive counters read as eight 16-byte
+// vectors, a warp scans its threads' sums by shuffles, warp 0 the 32 warp sums.
 __global__ void __launch_bounds__(1024) cell_scan_kernel(int32_t* __restrict__ counts_all) {
-  int32_t* __restrict__ counts = counts_all + (int64_t)blockIdx.x * kOrderCells;
-  constexpr int kPer = kOrderCells / 1024;
-  __shared__ int32_t part[1024];
-  int32_t local[kPer];
+  static_assert(kOrderCells == 1024 * 32, "one thread per 32 counters");
+  int4* __restrict__ counts = reinterpret_cast<int4*>(counts_all + (int64_t)blockIdx.x * kOrderCells);
+  __shared__ int32_t warp_sum[32];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  int4 v[8];
   int32_t s = 0;
-  const int t = threadIdx.x;
 #pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    local[i] = counts[t * kPer + i];
-    s += local[i];
+  for (int i = 0; i < 8; ++i) {
+    v[i] = counts[t * 8 + i];
+    s += v[i].x + v[i].y + v[i].z + v[i].w;
   }
-  part[t] = s;
+  int32_t incl = s;  // inclusive scan of the thread sums within the warp
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int32_t u = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += u;
+  }
+  if (lane == 31) warp_sum[warp] = incl;
   __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    const int32_t v = t >= off ? part[t - off] : 0;
-    __syncthreads();
-    part[t] += v;
-    __syncthreads();
-  }
-  int32_t run = part[t] - s;  // exclusive
+  if (warp == 0) {
+    int32_t w = warp_sum[lane];
 #pragma unroll
-  for (int i = 0; i < kPer; ++i) {
-    counts[t * kPer + i] = run;
-    run += local[i];
+    for (int off = 1; off < 32; off <<= 1) {
+      const int32_t u = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += u;
+    }
+    warp_sum[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  int32_t run = (warp > 0 ? warp_sum[warp - 1] : 0) + incl - s;  // exclusive start of this thread
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    int4 o;
+    o.x = run;
+    run += v[i].x;
+    o.y = run;
+    run += v[i].y;
+    o.z = run;
+    run += v[i].z;
+    o.w = run;
+    run += v[i].w;
+    counts[t * 8 + i] = o;
   }
 }
 
