@@ -18,7 +18,14 @@ struct Stage {
   int64_t pidx[32];  // point index of each lane (-1: no point)
 };
 
-__device__ __forceinline__ uint64_t bits_of(double x) { return static_cast<uint64_t>(__double_as_longlong(x)); }
+// The bit pattern of x through an opaque move: the compiler would otherwise turn tests such as
+// (bits << 1) == 0 or bits == bits(1.0) back into FP64 compares, which run on the FP64 pipe
+// (2.4 per AO in the split-BF16 planes kernel, 16 % of its FP64 instructions).
+__device__ __forceinline__ uint64_t bits_of(double x) {
+  uint64_t r;
+  asm("mov.b64 %0, %1;" : "=l"(r) : "d"(x));
+  return r;
+}
 __device__ __forceinline__ bool is_one(double f) { return bits_of(f) == 0x3FF0000000000000ull; }
 
 // ---------------------------------------------------------------- exponential
