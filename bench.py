@@ -170,8 +170,9 @@ def ncu_traffic():
             if line.startswith("kernel="):
                 kv = dict(t.split("=", 1) for t in line.split())
                 out[kv["kernel"]] = float(kv["dram_bytes_per_point"])
-                if "fp64_pipe_active" in kv:
-                    pipe[kv["kernel"]] = float(kv["fp64_pipe_active"])
+                for key in ("fp64_pipe_active", "tensor_pipe_active"):
+                    if key in kv:
+                        pipe.setdefault(kv["kernel"], {})[key + "_ncu"] = float(kv[key])
     return out, pipe
 
 
@@ -570,9 +571,8 @@ def main():
                 out[k] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                           "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
                 out[k]["frac"] = out[k]["achieved"] / peaks["hbm_gbs"]
-                if k in fp64_pipe:
-                    # what actually bounds it on GB300: FP64 issue (ncu, profiles/ao_vgl_fused_medium.md)
-                    out[k]["fp64_pipe_active_ncu"] = fp64_pipe[k]
+                # what actually bounds it on GB300: FP64 issue (ncu, profiles/ao_vgl_fused_medium.md)
+                out[k].update(fp64_pipe.get(k, {}))
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
             if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]
@@ -582,6 +582,12 @@ def main():
                 out[k] = {"bound": "tensor", "achieved": flops / (ms * 1e-3) / 1e12, "peak": pk, "unit": "TFLOP/s",
                           "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
                 out[k]["frac"] = out[k]["achieved"] / pk
+                out[k].update(fp64_pipe.get(k, {}))
+                if k == "mo_vgl_split_bf16":
+                    # the split executes six BF16 products per algorithmic one (on 64-padded K and
+                    # 16-padded column tiles); the algorithmic figure above counts 10 A M per point
+                    out[k]["bf16_products"] = 6
+                    out[k]["bf16_work_frac"] = 6.0 * out[k]["frac"]
         return out
 
     rf = {f: roof(f) for f in forms}
