@@ -296,7 +296,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
     et[0].hi[j] = (double)v;
     et[0].lo[j] = (double)(v - (long double)et[0].hi[j]);
   }
-  for (int j = 0; j < 256; ++j) et[0].fine[j] = (double)exp2l((long double)j / 256.0L);
+  for (int j = 0; j < kFine; ++j) et[0].fine[j] = (double)exp2l((long double)j / (long double)kFine);
   // the split-BF16 form's folded primitives: every exponent positive and finite, every
   // coefficient zero or of binary exponent within +-900 (so that sign * 2^k * e^y stays a
   // normal double over the active range y in [-27.7, ln 2))

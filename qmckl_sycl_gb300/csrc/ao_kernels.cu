@@ -67,7 +67,7 @@ __host__ __device__ constexpr int min_ctas() {
 // of the split-BF16 form), then the per-warp staging buffers.
 template <Out O>
 __host__ __device__ constexpr size_t stage_offset() {
-  return O == Out::Planes ? 512 + 2048 : 512;
+  return O == Out::Planes ? 512 + 8 * kFine : 512;
 }
 
 // ---------------------------------------------------------------- output staging
@@ -119,29 +119,28 @@ __device__ __forceinline__ double neg_int_to_double(int n) {
   return __longlong_as_double((long long)((b | sg) & (u == 0 ? 0ull : ~0ull)));
 }
 
-constexpr float kInvL256f = 369.32993f;                  // 256 / ln 2 (only picks the table index)
-constexpr double kL256 = 0.6931471805599453094 / 256.0;  // double nearest ln 2, / 256 (exact)
+constexpr float kInvLFinef = (float)(kFine / 0.6931471805599453094);  // kFine / ln 2 (picks the index)
+constexpr double kLFine = 0.6931471805599453094 / kFine;  // double nearest ln 2, / kFine (exact)
 
 // One primitive of the split-BF16 form: v = coef * e^(-expo r2) = sign * 2^k * e^y with
-// y = ln(mant) - expo r2 in FP64 (one fused multiply-add). e^y = 2^(n>>8) 2^((n&255)/256) e^r,
-// r = y - n ln2/256: n comes from an FP32 estimate of y (|r| <= ln2/512 + 1e-5 on the active
+// y = ln(mant) - expo r2 in FP64 (one fused multiply-add). e^y = 2^(n>>11) 2^((n&2047)/2048) e^r,
+// r = y - n ln2/2048: n comes from an FP32 estimate of y (|r| <= ln2/4096 + 1.2e-5 on the active
 // range y in [-27.7, ln 2)), -n is formed exactly with integer instructions, e^r - 1 by a
-// degree-4 polynomial (truncation 4e-17), 2^(j/256) from a 256-entry table, and the power of
-// two and the sign by integer addition: 9 FP64 instructions against 14 for coef * e^-(expo r2)
-// with the 32-entry method. The relative error stays within a few units of 1e-16 |y|.
+// degree-3 polynomial (truncation 4e-17), 2^(j/2048) from a 2048-entry table in shared memory,
+// and the power of two and the sign by integer addition: 7 FP64 instructions against 14 for
+// coef * e^-(expo r2) with the 32-entry method. The relative error stays within a few units of
+// 1e-16 |y|.
 __device__ __forceinline__ double fold_value(const PrimFold* __restrict__ F, double r2, float r2f,
                                              const double* __restrict__ fine) {
   const float yf = fmaf(__ldg(&F->naf), r2f, __ldg(&F->lnmf));
-  const float tf = fmaf(yf, kInvL256f, 12582912.0f);  // 1.5 * 2^23: rounds to an integer
+  const float tf = fmaf(yf, kInvLFinef, 12582912.0f);  // 1.5 * 2^23: rounds to an integer
   const int n = __float_as_int(tf) - 0x4B400000;
   const double y = fma(__ldg(&F->na), r2, __ldg(&F->lnm));
-  const double r = fma(neg_int_to_double(n), kL256, y);
-  double q = fma(r, 1.0 / 24.0, 1.0 / 6.0);
-  q = fma(q, r, 0.5);
-  const double p = fma(r * r, q, r);  // e^r - 1
-  const double th = fine[n & 255];
+  const double r = fma(neg_int_to_double(n), kLFine, y);
+  const double p = fma(r * r, fma(r, 1.0 / 6.0, 0.5), r);  // e^r - 1
+  const double th = fine[n & (kFine - 1)];
   const double e = fma(th, p, th);
-  const unsigned long long m = (unsigned long long)(long long)((n >> 8) + __ldg(&F->k));
+  const unsigned long long m = (unsigned long long)(long long)((n >> kFineBits) + __ldg(&F->k));
   const unsigned long long b = (unsigned long long)__double_as_longlong(e) + (m << 52);
   return __longlong_as_double((long long)(b ^ ((unsigned long long)__ldg(&F->sign) << 32)));
 }
@@ -675,7 +674,7 @@ struct CtaSmem {
     fine = thi + 64;  // split-BF16 planes only
     load_exp_table(tab->hi, tab->lo, thi, tlo);
     if constexpr (O == Out::Planes)
-      for (int i = threadIdx.x; i < 256; i += blockDim.x) fine[i] = tab->fine[i];
+      for (int i = threadIdx.x; i < kFine; i += blockDim.x) fine[i] = tab->fine[i];
     st = reinterpret_cast<Stage<ncomp<O>()>*>(raw + stage_offset<O>()) + warp;
     ebuf = reinterpret_cast<double*>(raw + fused_smem<O>(0)) + (size_t)warp * 32 * (ent_cap > 0 ? ent_cap : 0);
   }

@@ -62,11 +62,13 @@ struct NucleusChunk {
 
 // 2^(j/32), j = 0..31, as hi + lo doubles (hi = the double nearest to the value): the table of
 // the AO kernel's exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989).
-// fine[j] = the double nearest to 2^(j/256), the table of the split-BF16 form's primitive values.
+// fine[j] = the double nearest to 2^(j/kFine), the table of the split-BF16 form's primitive values.
+constexpr int kFineBits = 11;
+constexpr int kFine = 1 << kFineBits;
 struct ExpTable {
   double hi[32];
   double lo[32];
-  double fine[256];
+  double fine[kFine];
 };
 
 // A primitive of the packed list prepared for the split-BF16 form's radials, which evaluate
