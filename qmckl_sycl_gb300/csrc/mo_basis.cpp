@@ -1,6 +1,7 @@
 // MO basis: setters/getters (src/qmckl_mo.cpp:459-583 of qmckl_sycl), finalize
 // (coefficient transpose, src/qmckl_mo_sycl.cpp:137-189), select_mo (src/qmckl_mo.cpp:31-106)
 // and the provide chain for mo_vgl / mo_value (src/qmckl_mo.cpp:114-453).
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -219,6 +220,9 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
   if (mo.provided && ctx->ao_basis.provided && ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE &&
       ctx->point.date > mo.mo_vgl_date && ctx->point.num >= 16384 && mo_vgl &&
       size_max >= 5 * ctx->point.num * mo.mo_num && ensure_device(ctx) && host_memory(mo_vgl)) {
+    // four chunks: measured on 40960 points (medium workload) 4.81 / 3.79 / 3.32 / 3.48 ms per
+    // step for 1 / 2 / 4 / 8 chunks (the ~193 GB/s device-to-host link needs 2.54 ms for the
+    // 491 MB of mo_vgl; smaller chunks lose more to kernel tails than they gain in overlap)
     qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, 4);
     if (rc != QMCKL_SUCCESS_DEVICE) return rc;
     mo.mo_vgl_date = ctx->date;

@@ -35,6 +35,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "internal.hpp"
 
@@ -916,31 +917,33 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
     cudaGetLastError();
     return fail(c, QMCKL_FAILURE_DEVICE, fn, "stream creation failed");
   }
-  if (!ensure_raw(ctx, &mo.split_job, &mo.split_job_cap, sizeof(SplitJob)))
+  const int nc = (int)((P + pc - 1) / pc);
+  if (!ensure_raw(ctx, &mo.split_job, &mo.split_job_cap, sizeof(SplitJob) * (size_t)nc))
     return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptor");
   __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
+  // every chunk's job up front, in one upload: a descriptor copy per chunk from pageable memory
+  // would make the host wait for the stream between chunks
+  std::vector<SplitJob> jobs((size_t)nc);
+  std::vector<int> tiles((size_t)nc);
+  for (int k = 0; k < nc; ++k) {
+    const int64_t off = k * pc, n = P - off < pc ? P - off : pc;
+    tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 32), n, ao.point_perm,
+                           static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
+    if (tiles[k] < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
+  }
+  SplitJob* d_jobs = static_cast<SplitJob*>(mo.split_job);
+  cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SplitJob) * (size_t)nc, cudaMemcpyHostToDevice,
+                                  ctx->stream);
   cudaEvent_t done[16];
-  const int nc = (int)((P + pc - 1) / pc);
   for (int k = 0; k < nc; ++k) cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
-  cudaError_t e = cudaSuccess;
   for (int k = 0; k < nc && e == cudaSuccess; ++k) {
     const int64_t off = k * pc, n = P - off < pc ? P - off : pc;
     const double* coord = ctx->point.coord + off;  // rows of [3][P], slice of n points
     launch_point_order(ctx, ao.tables, coord, P, n, ao.point_keys, ao.cell_counts, ao.point_perm);
     launch_ao_planes(ctx, ao.tables, coord, P, ao.point_perm, n, kp, ap);
-    SplitJob job;
-    const int tiles = make_job_mn(job, ap, round_up(n, 32), n, ao.point_perm,
-                                  static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
-    if (tiles < 0) {
-      e = cudaErrorInvalidValue;
-      break;
-    }
-    // the descriptor upload is ordered after the previous chunk's contraction on this stream
-    e = cudaMemcpyAsync(mo.split_job, &job, sizeof job, cudaMemcpyHostToDevice, ctx->stream);
-    if (e != cudaSuccess) break;
     {
       LaunchScope scope(ctx, "mo_vgl_split_bf16");
-      launch_split_jobs(ctx->stream, static_cast<const SplitJob*>(mo.split_job), 1, tiles, err);
+      launch_split_jobs(ctx->stream, d_jobs + k, 1, tiles[k], err);
     }
     cudaEventRecord(done[k], ctx->stream);
     cudaStreamWaitEvent(ctx->copy_stream, done[k], 0);
