@@ -571,7 +571,7 @@ def main():
                 out[k] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                           "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
                 out[k]["frac"] = out[k]["achieved"] / peaks["hbm_gbs"]
-                # what actually bounds it on GB300: FP64 issue (ncu, profiles/ao_vgl_fused_medium.md)
+                # what actually bounds it on GB300: FP64 issue (the FP64-pipe activity ncu measured)
                 out[k].update(fp64_pipe.get(k, {}))
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
             if st.get(k, (0, 0))[0] > 0:
