@@ -22,10 +22,33 @@ def run(s, mode):
         return dict(ao_vgl=ctx.get_ao_vgl(P), mo_vgl=ctx.get_mo_vgl(P), mo_value=ctx.get_mo_value(P))
 
 
-@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium_sub"])
+def _replace(s, **kw):
+    return s.__class__(**{**s.__dict__, **kw})
+
+
+def _unfoldable():
+    # a coefficient outside the folded evaluation's range (2^-900): the planes kernel evaluates
+    # the radials like the FP64 form
+    s = config_small(6, point_num=200)
+    c = s.coefficient.copy()
+    c[3] = 1e-300
+    return _replace(s, coefficient=c)
+
+
+def _signed():
+    # negative and zero coefficients (the folded evaluation's sign bit and never-active entries)
+    s = config_small(8, point_num=200)
+    c = s.coefficient.copy()
+    c[1::3] *= -1.0
+    c[::11] = 0.0
+    return _replace(s, coefficient=c)
+
+
+@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium_sub", "unfoldable", "signed"])
 def test_split_mo_vgl_within_1e6(name, chbrclf):
     s = {"chbrclf": lambda: chbrclf, "small": lambda: config_small(0), "adjoint": lambda: config_adjoint(0),
-         "medium_sub": lambda: config_medium(0, walkers=8, electrons=160)}[name]()
+         "medium_sub": lambda: config_medium(0, walkers=8, electrons=160), "unfoldable": _unfoldable,
+         "signed": _signed}[name]()
     ref = oracle.forward(s, want=("ao_vgl", "mo_vgl", "mo_value"))
     out = run(s, PRECISION_SPLIT_BF16)
     assert normwise_rel_err(out["ao_vgl"], ref["ao_vgl"]) <= 1e-12
