@@ -285,7 +285,7 @@ qmckl_exit_code_device build_descriptors(Batch* b, const std::vector<Member>& ms
   int64_t tiles = 0;
   if (split) {
     split_jobs.assign(jb * (size_t)n, 0);
-    const int n_cap = b->tune.v[2] < 0 ? 96 : b->tune.v[2];
+    const int n_cap = b->tune.v[2] < 0 ? 160 : b->tune.v[2];
     for (int i = 0; i < n; ++i) {
       const Member& e = ms[g_order[i]];
       const int t = split_make_job_mn(split_jobs.data() + jb * i, e.planes, (e.P + 31) / 32 * 32, e.P,
@@ -486,8 +486,8 @@ qmckl_exit_code_device autotune(Batch* b, const std::vector<Member>& ms) {
   // contraction tile
   best = 1e300;
   if (split) {
-    int best_cap = 96;
-    const int caps[] = {96, 64, 48, 32};
+    int best_cap = 160;
+    const int caps[] = {160, 128, 96, 64};
     for (int cap : caps) {
       b->tune.v[2] = cap;
       rc = build_descriptors(b, ms);

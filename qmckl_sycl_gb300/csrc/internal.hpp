@@ -439,7 +439,7 @@ cudaError_t launch_dgemm_batch(cudaStream_t stream, int shape, bool mask5, const
 // Split-BF16 contraction of several molecules: host-built descriptors (opaque here).
 size_t split_job_bytes();
 // Writes one job (out[rows][M] from A planes [3][rows][kp] and B planes [3][M][kp]) into
-// job_host with column tiles of at most n_cap (16..96) columns; returns its tile count or -1.
+// job_host with column tiles of at most n_cap (16..160) columns; returns its tile count or -1.
 int split_make_job(void* job_host, const void* a_planes, int64_t rows, const void* b_planes, int64_t M, int64_t kp,
                    double* out, int tile_begin, int n_cap);
 // The same from the fused AO kernel's M-major planes ([3][kp][5 pp]; see launch_ao_planes) into

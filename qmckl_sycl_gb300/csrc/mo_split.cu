@@ -18,19 +18,23 @@
 // Accumulation. The tensor core adds each MMA's products into the FP32 accumulator with a
 // truncating alignment, so every MMA costs an error of order 2^-24 of the accumulator (and of
 // its largest product). The five correction products (all ~2^-8 of the result or smaller)
-// go into their own accumulator; the main hi*hi product is accumulated for one 64-wide K
-// block at a time (four MMAs) in one of two ping-pong buffers, and the epilogue warps fold
-// each finished block into a running FP32 two-sum (hi, lo) kept in tensor memory while the
-// next block is multiplied. The error therefore does not grow with K. The FP64 result is
-// hi + lo + corrections, formed with a single FP64 addition.
+// go into their own accumulator; the main hi*hi product is accumulated for two 64-wide K
+// blocks at a time (eight MMAs) in one of two alternating tensor-memory buffers, and the fold
+// warps add each finished block sum into a running FP32 two-sum (hi, lo) held in registers
+// while the next blocks are multiplied. The error therefore does not grow with K. The result
+// is hi + (lo + corrections), rounded once to FP32 and widened exactly to FP64.
 //
-// GEMM structure (one 128 x N output tile per CTA, N <= 96): warp 0 issues TMA loads of the
-// six operand planes per 64-wide K block into a two-stage ring of 128B-swizzled shared
-// memory buffers; warp 1 owns tensor memory and issues the MMAs (24 per K block: six
-// products x four K=16 steps); warps 2-5 (each its 32-lane quarter of tensor memory) fold
-// the main product per block and finally store the FP64 results. Every mbarrier wait
-// is bounded (~1 s); on expiry the kernel records an error code, drains what it issued,
-// releases its tensor memory and exits, and the host reports QMCKL_FAILURE_DEVICE.
+// GEMM structure (persistent, one CTA per SM, 128 x N output tiles with N <= 160): warp 0
+// issues TMA loads of the six operand planes per 64-wide K block into a two-stage ring of
+// 128B-swizzled shared-memory buffers; warp 1 owns tensor memory and issues the MMAs (24 per K
+// block: six products x four K=16 steps); eight fold warps, two per 32-lane quarter of tensor
+// memory (one row per thread, one column half per warp), fold the main product and write the
+// tile's FP64 results through a small per-warp transposition buffer, so that each store
+// instruction covers four 64-byte row segments. An MMA costs nearly the same time for N = 32
+// to 128 (its A operand fetch dominates), so the widest tile that tensor memory and shared
+// memory allow sets the rate: 160 columns halve the MMA count of 80-column tiles. Every
+// mbarrier wait is bounded (~1 s); on expiry the kernel records an error code, drains what it
+// issued, releases its tensor memory and exits, and the host reports QMCKL_FAILURE_DEVICE.
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -45,16 +49,22 @@ namespace {
 constexpr int kBM = 128;        // rows per tile (UMMA M)
 constexpr int kBK = 64;         // K per stage: 64 BF16 = 128 bytes = one swizzle row
 constexpr int kStages = 2;
-constexpr int kMaxN = 96;       // columns per tile (the fold warps hold 2 x kMaxN sums per row)
-constexpr int kThreads = 384;   // 12 warps = 3 warpgroups: {TMA, MMA, 2 idle}, 4 fold warps, 4 store warps
-constexpr int kBufs = 3;         // main-product TMEM buffers: the MMAs run up to two fold groups ahead
+constexpr int kMaxN = 160;      // columns per tile: two halves of <= 80, each fold thread holds 2 x 80 sums
+constexpr int kHalfN = kMaxN / 2;
+constexpr int kThreads = 384;   // 12 warps = 3 warpgroups: {TMA, MMA, 2 idle}, 8 fold warps
+constexpr int kBufs = 2;         // main-product TMEM buffers: the MMAs run up to one fold group ahead
 constexpr int kFold = 2;         // K blocks (of 64) per main-product block sum folded into the two-sum
-// registers per thread after setmaxnreg: warpgroup 0 (TMA, MMA), 1 (fold), 2 (store); launched
-// with 168 per thread: 384 x 168 = 64512 >= 128 x (112 + 248 + 88) = 57344
-constexpr int kRegsIssue = 112;
-constexpr int kRegsFold = 248;
-constexpr int kRegsStore = 88;
+// Tensor memory (512 columns): corrections [0, kMaxN), main buffer b at kMaxN * (1 + b).
+static_assert(kMaxN * (1 + kBufs) <= 512, "tensor memory holds the corrections and the main buffers");
+// registers per thread after setmaxnreg: warpgroup 0 (TMA, MMA), warpgroups 1 and 2 (fold);
+// launched with 168 per thread: 384 x 168 = 64512 = 128 x 56 + 256 x 224
+constexpr int kRegsIssue = 56;
+constexpr int kRegsFold = 224;
+static_assert(128 * kRegsIssue + 256 * kRegsFold <= kThreads * 168, "register split exceeds the launch's registers");
 constexpr uint32_t kPlaneA = kBM * kBK * 2;  // 16 KB per A plane and stage
+constexpr uint32_t kMaxStage = 3 * kPlaneA + 3 * (uint32_t)kMaxN * kBK * 2;  // 108 KB
+constexpr int kTPitch = 9;                   // transposition buffer: 32 rows x 8 floats, row pitch 9
+constexpr uint32_t kTBuf = 32 * kTPitch * 4;  // bytes per fold warp
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
 
 // ------------------------------------------------------------------ split helpers
@@ -256,6 +266,11 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bp)) + (b - bp);
 }
 
+// One 32-byte store (four doubles) to a 32-byte aligned global address.
+__device__ __forceinline__ void st_global_v4(double* p, double a, double b, double c, double d) {
+  asm volatile("st.global.v4.f64 [%0], {%1, %2, %3, %4};" ::"l"(p), "d"(a), "d"(b), "d"(c), "d"(d) : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
@@ -284,9 +299,6 @@ __device__ __forceinline__ void set_abort(volatile int* abort_flag, int* error, 
   *abort_flag = 1;
   atomicExch(error, code);
 }
-
-// Output staging of the epilogue: 4 warps x 32 rows x (kMaxN + 1) FP32 values.
-constexpr uint32_t kOutStage = 4 * 32 * (kMaxN + 1) * 4;
 
 // Tile geometry of launch tile `tile`: its job and the job-local row / column origins.
 struct TileRef {
@@ -318,23 +330,41 @@ __device__ __forceinline__ void reg_inc() { asm volatile("setmaxnreg.inc.sync.al
 // What the fold warps of a CTA share across tiles.
 struct FoldCtx {
   uint32_t lb;                       // TMEM address of this warp's 32 lanes, column 0
-  float* stg;                        // this warp's 32 rows of the output staging buffer
-  uint64_t *accf, *acce, *tmem_free, *out_ready, *out_free;
+  float* tb;                         // this warp's transposition buffer (32 rows x kTPitch)
+  uint64_t *accf, *acce, *tmem_free;
   volatile int* abort_flag;
   int* error;
-  int lane;
+  int lane, quarter, half;
 };
 
-// The fold warps' work on one tile of N columns (one row per thread): after every kFold K
-// blocks, the main product's FP32 block sum from TMEM is added into a running two-sum (hi, lo) held in
-// registers (a TMEM round trip of hi and lo per K block would add 4N column accesses to the N
-// of the main buffer, and tensor-memory traffic slows the MMAs that share it: 20 % of the
-// kernel's time on the medium workload); at the end hi + (lo + corrections) goes to the staging
-// buffer. it: the running fold-group index (advanced), tl: the CTA's tile count. Returns false
-// when a wait gave up.
-__device__ __forceinline__ bool fold_tile(const FoldCtx& f, int N, int kblocks, uint32_t& it, uint32_t tl) {
-  float rhi[kMaxN], rlo[kMaxN];
-  const int groups = (kblocks + kFold - 1) / kFold;
+// Reads n (16 or 8) consecutive columns of the warp's 32 lanes from tensor memory and waits.
+__device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, bool full16, uint32_t (&r)[16]) {
+  if (full16) {
+    tmem_ld16_async(taddr, r);
+  } else {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int q = 8; q < 16; ++q) r[q] = 0u;
+  }
+  tmem_wait_ld(r);
+}
+
+// One fold warp's work on one tile (one row per thread, this warp's half of the N columns):
+// after every kFold K blocks, the main product's FP32 block sum is read out of tensor memory and
+// added into a running two-sum (hi, lo) held in registers (tensor-memory traffic slows the MMAs
+// that share it, so the two-sum does not live there); at the end hi + (lo + corrections) is
+// formed, tensor memory is released to the next tile, and the warp writes its 32 x N/2 block of
+// the output: with 32-byte stores of each lane's own row where the rows allow it, otherwise eight
+// columns at a time through the transposition buffer (each store instruction then writes four
+// rows x 64 contiguous bytes). it: the running fold-group index (advanced). Returns false when a
+// wait gave up.
+__device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job, const TileRef& tr, uint32_t& it) {
+  float rhi[kHalfN], rlo[kHalfN];
+  const int nh = job.n_tile >> 1;             // columns of this warp: [hc, hc + nh)
+  const uint32_t hc = (uint32_t)(f.half * nh);
+  const int groups = (job.kblocks + kFold - 1) / kFold;
   for (int kb = 0; kb < groups; ++kb, ++it) {
     const uint32_t b = it % kBufs, use = it / kBufs;
     // warp-uniform decision: the tcgen05.ld below are .sync.aligned
@@ -343,22 +373,25 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, int N, int kblocks, 
       return false;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t mcol = (uint32_t)kMaxN * (1 + b) + hc;
 #pragma unroll
-    for (int c0 = 0; c0 < kMaxN; c0 += 16) {
-      if (c0 < N) {
+    for (int c0 = 0; c0 < kHalfN; c0 += 16) {
+      if (c0 < nh) {
+        const bool full16 = c0 + 16 <= nh;
         uint32_t rv[16];
-        tmem_ld16_async(f.lb + (1 + b) * (uint32_t)N + (uint32_t)c0, rv);
-        tmem_wait_ld(rv);
+        tmem_ld_cols(f.lb + mcol + (uint32_t)c0, full16, rv);
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
-          if (kb == 0) {
-            rhi[c0 + q] = __uint_as_float(rv[q]);
-            rlo[c0 + q] = 0.f;
-          } else {
-            float s2, e2;
-            two_sum(rhi[c0 + q], __uint_as_float(rv[q]), s2, e2);
-            rhi[c0 + q] = s2;
-            rlo[c0 + q] += e2;
+          if (q < 8 || full16) {
+            if (kb == 0) {
+              rhi[c0 + q] = __uint_as_float(rv[q]);
+              rlo[c0 + q] = 0.f;
+            } else {
+              float s2, e2;
+              two_sum(rhi[c0 + q], __uint_as_float(rv[q]), s2, e2);
+              rhi[c0 + q] = s2;
+              rlo[c0 + q] += e2;
+            }
           }
         }
       }
@@ -367,64 +400,102 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, int N, int kblocks, 
     __syncwarp();
     if (f.lane == 0) mbar_arrive(&f.acce[b]);
   }
-  // The last accf phase covered every MMA of the tile, corrections included: read the
-  // corrections out into the staging buffer with the two-sum (once the store warps have written
-  // out the previous tile), then release tensor memory to the next tile and the staging buffer
-  // to the store warps.
-  if (tl > 0 && !__all_sync(0xffffffffu, wait_or_abort(f.out_free, (tl - 1) & 1u, f.abort_flag))) {
-    if (f.lane == 0) set_abort(f.abort_flag, f.error, 7);
-    return false;
-  }
-  const int pitch = kMaxN + 1;  // odd pitch spreads the rows over the banks
+  // The last accf phase covered every MMA of the tile, corrections included.
 #pragma unroll
-  for (int c0 = 0; c0 < kMaxN; c0 += 16) {
-    if (c0 < N) {
+  for (int c0 = 0; c0 < kHalfN; c0 += 16) {
+    if (c0 < nh) {
+      const bool full16 = c0 + 16 <= nh;
       uint32_t rc[16];
-      tmem_ld16_async(f.lb + (uint32_t)c0, rc);
-      tmem_wait_ld(rc);
+      tmem_ld_cols(f.lb + hc + (uint32_t)c0, full16, rc);
 #pragma unroll
       for (int q = 0; q < 16; ++q) {
-        float s2, e2;
-        two_sum(rhi[c0 + q], __uint_as_float(rc[q]), s2, e2);
-        // hi + (lo + e) rounded once to FP32 (2^-24 relative)
-        f.stg[f.lane * pitch + c0 + q] = s2 + (rlo[c0 + q] + e2);
+        if (q < 8 || full16) {
+          float s2, e2;
+          two_sum(rhi[c0 + q], __uint_as_float(rc[q]), s2, e2);
+          rhi[c0 + q] = s2 + (rlo[c0 + q] + e2);  // hi + (lo + e) rounded once to FP32 (2^-24 relative)
+        }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncwarp();
-  if (f.lane == 0) {
-    mbar_arrive(f.tmem_free);
-    mbar_arrive(f.out_ready);
+  if (f.lane == 0) mbar_arrive(f.tmem_free);  // the next tile's MMAs may overwrite tensor memory
+
+  // Output rows of the warp's 32 tile rows (lane = row).
+  const int64_t row = (int64_t)tr.m0 + f.quarter * 32 + f.lane;
+  int64_t orow = row < job.rows ? row : -1;
+  if (job.a_mn && orow >= 0) {
+    const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+    orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
+  }
+  const int64_t c_first = (int64_t)tr.n0 + hc;  // first output column of this warp
+  const int ncol = (int)(job.cols - c_first < nh ? job.cols - c_first : nh);  // valid columns (may be <= 0)
+  if ((reinterpret_cast<uintptr_t>(job.out) & 31) == 0 && (job.ldo & 3) == 0 && (c_first & 3) == 0) {
+    // 32-byte aligned row segments: each lane writes its own row, four columns per 32-byte
+    // store, straight from registers (shared memory is busy with the MMAs' operand reads and
+    // the TMA fills at this point, and waiting for it costs more than the scattered sectors).
+    if (orow >= 0) {
+      double* __restrict__ const p = job.out + orow * job.ldo + c_first;
+#pragma unroll
+      for (int c0 = 0; c0 < kHalfN; c0 += 4) {
+        if (c0 + 4 <= ncol) {
+          st_global_v4(p + c0, f32_to_f64_int(rhi[c0]), f32_to_f64_int(rhi[c0 + 1]), f32_to_f64_int(rhi[c0 + 2]),
+                       f32_to_f64_int(rhi[c0 + 3]));
+        } else if (c0 < ncol) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (c0 + j < ncol) p[c0 + j] = f32_to_f64_int(rhi[c0 + j]);
+        }
+      }
+    }
+    return true;
+  }
+  // Otherwise (unaligned rows): eight columns at a time through the transposition buffer.
+  const int rr = f.lane >> 3, cc = f.lane & 7;  // read-back: rows rr + 4 i, column cc of the 8
+  // The job's fields in registers: the stores below could alias them for the compiler, which
+  // would otherwise reload them from global memory after every store.
+  double* __restrict__ const out = job.out + c_first + cc;
+  const int64_t ldo = job.ldo;
+  float* __restrict__ const tb = f.tb;
+  int64_t orows[8];  // output row of each read-back row, -1 where there is none
+#pragma unroll
+  for (int i = 0; i < 8; ++i) orows[i] = __shfl_sync(0xffffffffu, orow, 4 * i + rr);
+#pragma unroll
+  for (int c0 = 0; c0 < kHalfN; c0 += 8) {
+    if (c0 < ncol) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) tb[f.lane * kTPitch + j] = rhi[c0 + j];
+      __syncwarp();
+      const bool col_ok = c0 + cc < ncol;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const float v = tb[(4 * i + rr) * kTPitch + cc];
+        if (orows[i] >= 0 && col_ok) out[orows[i] * ldo + c0] = f32_to_f64_int(v);
+      }
+      __syncwarp();
+    }
   }
   return true;
 }
 
-// Tensor-memory columns: [0,N) corrections, then kBufs main-product buffers of N columns (one
-// 64-wide K block each, rotating), folded into the fold warps' register two-sum after every K
-// block.
-//
 // Persistent and continuous: CTA b processes tiles b, b + gridDim.x, ... of the launch (tiles
 // of one job are ordered column tile fastest, so CTAs running at the same time share A rows in
 // L2). The three roles walk the same sequence of (tile, K block) steps with running barrier
-// phases, so the producer prefetches the next tile while the epilogue finishes the current one;
-// the only hand-over between tiles is `tmem_free`: the MMA issuer starts a tile once the
-// epilogue has read the previous tile's accumulators out of tensor memory (the epilogue then
-// writes that tile's output from its own staging buffer while the next tile computes).
+// phases, so the producer prefetches the next tile while the fold warps finish the current one;
+// the only hand-over between tiles is `tmem_free`: the MMA issuer starts a tile once the fold
+// warps have read the previous tile's corrections out of tensor memory (they then write that
+// tile's output while the next tile computes).
 __global__ void __launch_bounds__(kThreads, 1)
     split_gemm_kernel(const SplitJob* __restrict__ jobs, int njobs, int total_tiles, int* error) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const uint32_t max_stage = 3 * kPlaneA + 3 * (uint32_t)kMaxN * kBK * 2;
-  float* out_stage = (float*)(base + kStages * max_stage);
-  uint64_t* full = (uint64_t*)(base + kStages * max_stage + kOutStage);
+  float* tbuf = (float*)(base + kStages * kMaxStage);
+  uint64_t* full = (uint64_t*)(base + kStages * kMaxStage + 8 * kTBuf);
   uint64_t* empty = full + kStages;
-  uint64_t* accf = empty + kStages;  // [kBufs] main buffer filled (MMA -> epilogue)
-  uint64_t* acce = accf + kBufs;     // [kBufs] main buffer folded (epilogue -> MMA)
-  uint64_t* tmem_free = acce + kBufs;  // accumulators of the last tile read out (epilogue -> MMA)
-  uint64_t* out_ready = tmem_free + 1;  // staging buffer filled (fold warps -> store warps)
-  uint64_t* out_free = out_ready + 1;   // staging buffer written out (store warps -> fold warps)
-  uint64_t* mma_done = out_free + 1;
+  uint64_t* accf = empty + kStages;  // [kBufs] main buffer filled (MMA -> fold warps)
+  uint64_t* acce = accf + kBufs;     // [kBufs] main buffer folded (fold warps -> MMA)
+  uint64_t* tmem_free = acce + kBufs;  // accumulators of the last tile read out (fold warps -> MMA)
+  uint64_t* mma_done = tmem_free + 1;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
   const uint32_t tmem_cols = 512;
@@ -443,11 +514,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < kBufs; ++b) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], 4);
+      mbar_init(&acce[b], 8);
     }
-    mbar_init(tmem_free, 4);
-    mbar_init(out_ready, 4);
-    mbar_init(out_free, 4);
+    mbar_init(tmem_free, 8);
     mbar_init(mma_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -455,7 +524,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  // Registers move from the producer/MMA and store warpgroups to the fold warpgroup; each role
+  // Registers move from the producer/MMA warpgroup to the two fold warpgroups; each role
   // adjusts its warpgroup's allocation on entry (all four warps of a warpgroup do the same).
   if (warp == 0) {
     reg_dec<kRegsIssue>();
@@ -475,7 +544,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             ok = false;
             break;
           }
-          unsigned char* st = base + s2 * max_stage;
+          unsigned char* st = base + s2 * kMaxStage;
           mbar_expect_tx(&full[s2], stage_bytes);
           if (job.a_mn) {
             // two 64(M) x 64(K) boxes per plane: M rows m0..m0+63, then m0+64..m0+127
@@ -510,7 +579,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                                ((uint32_t)(N >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
         const bool amn = job.a_mn != 0;
         const uint64_t ka = amn ? 128u : 2u, pa = kPlaneA >> 4, pb = plane_b >> 4;
-        // the correction accumulator and the previous tile's two-sum are read out before reuse
+        // the correction accumulator is read out before reuse
         if (tl > 0 && !wait_or_abort(tmem_free, (tl - 1) & 1u, abort_flag)) {
           set_abort(abort_flag, error, 6);
           break;
@@ -532,10 +601,10 @@ __global__ void __launch_bounds__(kThreads, 1)
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           // descriptors in 16-byte units: a K step is 2 (32 bytes along a K-major row) or 128
           // (16 rows of 128 bytes, M-major); planes are kPlaneA / plane_b bytes apart
-          const uint32_t sa = smem_u32(base + s2 * max_stage);
+          const uint32_t sa = smem_u32(base + s2 * kMaxStage);
           const uint64_t da = amn ? sdesc_mn(sa) : sdesc(sa);
           const uint64_t db = sdesc(sa + 3 * kPlaneA);
-          const uint32_t main_acc = tmem + (1 + b) * (uint32_t)N;
+          const uint32_t main_acc = tmem + (uint32_t)kMaxN * (1 + b);
 #pragma unroll
           for (int kk = 0; kk < kBK / 16; ++kk) {
             const uint64_t a = da + kk * ka, bb = db + kk * 2u;
@@ -555,55 +624,18 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
   } else if (warp < 4) {
     reg_dec<kRegsIssue>();  // warps 2 and 3: no role (they complete warpgroup 0)
-  } else if (warp < 8) {
+  } else {
     reg_inc();
     // ---------------- fold warps: warp w owns TMEM lanes 32*(w % 4) .. +31 (one row per thread)
-    const int quarter = warp & 3;
-    const uint32_t lb = tmem + ((uint32_t)(quarter * 32) << 16);
-    float* stg = out_stage + (size_t)quarter * 32 * (kMaxN + 1);
-    uint32_t it = 0, tl = 0;
+    // and column half (w - 4) / 4 of each tile
+    const int quarter = warp & 3, half = (warp - 4) >> 2;
+    FoldCtx f{tmem + ((uint32_t)(quarter * 32) << 16), tbuf + (size_t)(warp - 4) * 32 * kTPitch, accf, acce,
+              tmem_free, abort_flag, error, lane, quarter, half};
+    uint32_t it = 0;
     bool ok = true;
-    for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x, ++tl) {
+    for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
       const TileRef tr = tile_ref(jobs, njobs, tile);
-      const SplitJob& job = *tr.job;
-      FoldCtx f{lb, stg, accf, acce, tmem_free, out_ready, out_free, abort_flag, error, lane};
-      ok = fold_tile(f, job.n_tile, job.kblocks, it, tl);
-    }
-  } else {
-    reg_dec<kRegsStore>();
-    // ---------------- store warps: write each tile's staged rows as contiguous row segments
-    // (one thread per row would write 32 scattered 8-byte pieces per instruction)
-    const int quarter = warp & 3;
-    const float* stg = out_stage + (size_t)quarter * 32 * (kMaxN + 1);
-    const int pitch = kMaxN + 1;
-    uint32_t tl = 0;
-    for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x, ++tl) {
-      const TileRef tr = tile_ref(jobs, njobs, tile);
-      const SplitJob& job = *tr.job;
-      const int64_t row = (int64_t)tr.m0 + quarter * 32 + lane;
-      int64_t orow = row < job.rows ? row : -1;
-      if (job.a_mn && orow >= 0) {
-        const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
-        orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
-      }
-      if (!__all_sync(0xffffffffu, wait_or_abort(out_ready, tl & 1u, abort_flag))) break;
-      const int ncol = (int)(job.cols - tr.n0 < job.n_tile ? job.cols - tr.n0 : job.n_tile);
-      // rows four at a time, so that the shared loads and global stores of a lane overlap
-      for (int r0 = 0; r0 < 32; r0 += 4) {
-        int64_t orr[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) orr[u] = __shfl_sync(0xffffffffu, orow, r0 + u);
-        for (int c = lane; c < ncol; c += 32) {
-          double v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) v[u] = f32_to_f64_int(stg[(r0 + u) * pitch + c]);
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (orr[u] >= 0) job.out[orr[u] * job.ldo + tr.n0 + c] = v[u];
-        }
-      }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(out_free);
+      ok = fold_tile(f, *tr.job, tr, it);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -721,9 +753,7 @@ int make_job_mn(SplitJob& job, const __nv_bfloat16* ap, int64_t pp, int64_t npts
   return (int)((rows + kBM - 1) / kBM) * job.col_tiles;
 }
 
-size_t split_smem_bytes() {
-  return 1024 + kStages * (3 * (size_t)kPlaneA + 3 * (size_t)kMaxN * kBK * 2) + kOutStage + 256;
-}
+size_t split_smem_bytes() { return 1024 + kStages * (size_t)kMaxStage + 8 * (size_t)kTBuf + 256; }
 
 // One persistent launch over every tile of the njobs jobs at d_jobs (device memory).
 cudaError_t launch_split_jobs(cudaStream_t stream, const SplitJob* d_jobs, int njobs, int total_tiles, int* err) {
