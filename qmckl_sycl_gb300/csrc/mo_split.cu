@@ -364,6 +364,14 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
   float rhi[kHalfN], rlo[kHalfN];
   const int nh = job.n_tile >> 1;             // columns of this warp: [hc, hc + nh)
   const uint32_t hc = (uint32_t)(f.half * nh);
+  // Output row of this thread's tile row (lane = row), looked up before the folds so that the
+  // point order's load latency is hidden.
+  const int64_t row = (int64_t)tr.m0 + f.quarter * 32 + f.lane;
+  int64_t orow = row < job.rows ? row : -1;
+  if (job.a_mn && orow >= 0) {
+    const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+    orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
+  }
   const int groups = (job.kblocks + kFold - 1) / kFold;
   for (int kb = 0; kb < groups; ++kb, ++it) {
     const uint32_t b = it % kBufs, use = it / kBufs;
@@ -421,13 +429,6 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
   __syncwarp();
   if (f.lane == 0) mbar_arrive(f.tmem_free);  // the next tile's MMAs may overwrite tensor memory
 
-  // Output rows of the warp's 32 tile rows (lane = row).
-  const int64_t row = (int64_t)tr.m0 + f.quarter * 32 + f.lane;
-  int64_t orow = row < job.rows ? row : -1;
-  if (job.a_mn && orow >= 0) {
-    const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
-    orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
-  }
   const int64_t c_first = (int64_t)tr.n0 + hc;  // first output column of this warp
   const int ncol = (int)(job.cols - c_first < nh ? job.cols - c_first : nh);  // valid columns (may be <= 0)
   if ((reinterpret_cast<uintptr_t>(job.out) & 31) == 0 && (job.ldo & 3) == 0 && (c_first & 3) == 0) {
