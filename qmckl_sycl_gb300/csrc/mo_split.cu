@@ -85,14 +85,24 @@ __device__ __forceinline__ float f64_to_f32_int(double a) {
   return __uint_as_float(sign | bits);
 }
 
-// Float -> double exactly, by integer operations for normal numbers and zero.
+// Float -> double exactly, by integer operations only, for every input (normal, zero,
+// subnormal, infinity, NaN): a conversion instruction would run on the FP64 pipe, which issues at
+// 1/64 of the FP32 rate on this GPU (the epilogue converts every output element).
 __device__ __forceinline__ double f32_to_f64_int(float f) {
   const unsigned int u = __float_as_uint(f);
-  const unsigned int e = (u >> 23) & 0xFF;
-  if (e == 0 || e == 0xFF) return (double)f;  // zero, subnormal, inf, nan (rare)
-  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)(e + 896) << 52) |
-                                  ((unsigned long long)(u & 0x7FFFFF) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned int e = (u >> 23) & 0xFF, m = u & 0x7FFFFF;
+  unsigned long long bits;
+  if (e == 0) {
+    // zero, or the subnormal m 2^-149: its leading bit at position p becomes the implicit one
+    const int p = 31 - __clz(m);
+    bits = m == 0 ? 0ull
+                  : ((unsigned long long)(p + 874) << 52) | (((unsigned long long)m << (52 - p)) & 0xFFFFFFFFFFFFFull);
+  } else {
+    const unsigned long long ee = e == 0xFF ? 0x7FFull : (unsigned long long)(e + 896);
+    bits = (ee << 52) | ((unsigned long long)m << 29);
+  }
+  return __longlong_as_double((long long)(sign | bits));
 }
 
 __device__ __forceinline__ void split3(double a, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
@@ -337,6 +347,38 @@ struct FoldCtx {
   int lane, quarter, half;
 };
 
+// Starts reading 16 (full16) or 8 consecutive columns of the warp's 32 lanes from tensor memory
+// into r[o..o+15] (the rest of the 16 zeroed); tmem_wait_ld32 completes it.
+__device__ __forceinline__ void tmem_ld_async(uint32_t taddr, bool full16, uint32_t (&r)[32], int o) {
+  if (full16) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[o + 0]), "=r"(r[o + 1]), "=r"(r[o + 2]), "=r"(r[o + 3]), "=r"(r[o + 4]), "=r"(r[o + 5]),
+          "=r"(r[o + 6]), "=r"(r[o + 7]), "=r"(r[o + 8]), "=r"(r[o + 9]), "=r"(r[o + 10]), "=r"(r[o + 11]),
+          "=r"(r[o + 12]), "=r"(r[o + 13]), "=r"(r[o + 14]), "=r"(r[o + 15])
+        : "r"(taddr));
+  } else {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[o + 0]), "=r"(r[o + 1]), "=r"(r[o + 2]), "=r"(r[o + 3]), "=r"(r[o + 4]), "=r"(r[o + 5]),
+                   "=r"(r[o + 6]), "=r"(r[o + 7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int q = 8; q < 16; ++q) r[o + q] = 0u;
+  }
+}
+// Waits for every outstanding tcgen05.ld of the thread; the 32 registers pass through it so that
+// their uses cannot be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait_ld32(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                 "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                 "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
+}
+
 // Reads n (16 or 8) consecutive columns of the warp's 32 lanes from tensor memory and waits.
 __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, bool full16, uint32_t (&r)[16]) {
   if (full16) {
@@ -382,15 +424,18 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t mcol = (uint32_t)kMaxN * (1 + b) + hc;
+    // 32 columns per wait: two loads in flight halve the tensor-memory round trips
 #pragma unroll
-    for (int c0 = 0; c0 < kHalfN; c0 += 16) {
+    for (int c0 = 0; c0 < kHalfN; c0 += 32) {
       if (c0 < nh) {
-        const bool full16 = c0 + 16 <= nh;
-        uint32_t rv[16];
-        tmem_ld_cols(f.lb + mcol + (uint32_t)c0, full16, rv);
+        const bool fa = c0 + 16 <= nh, hb = c0 + 16 < nh, fb = c0 + 32 <= nh;
+        uint32_t rv[32];
+        tmem_ld_async(f.lb + mcol + (uint32_t)c0, fa, rv, 0);
+        if (hb) tmem_ld_async(f.lb + mcol + (uint32_t)c0 + 16, fb, rv, 16);
+        tmem_wait_ld32(rv);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          if (q < 8 || full16) {
+        for (int q = 0; q < 32; ++q) {
+          if (c0 + q < kHalfN && (q < 8 || (q < 16 && fa) || (q >= 16 && hb && (q < 24 || fb)))) {
             if (kb == 0) {
               rhi[c0 + q] = __uint_as_float(rv[q]);
               rlo[c0 + q] = 0.f;
