@@ -160,9 +160,9 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """Per-point DRAM bytes (and FP64-pipe activity, where measured) of the dominant kernels from
-    the committed ncu summary (profiles/ncu_traffic.txt, lines `kernel=<name>
-    dram_bytes_per_point=<x> [fp64_pipe_active=<f>]`)."""
+    """Per-point DRAM bytes (and FP64-pipe activity and FP64 thread instructions per point, where
+    measured) of the dominant kernels from the committed ncu summary (profiles/ncu_traffic.txt,
+    lines `kernel=<name> dram_bytes_per_point=<x> [fp64_pipe_active=<f>] [fp64_inst_per_point=<n>]`)."""
     out, pipe = {}, {}
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if os.path.exists(path):
@@ -170,7 +170,7 @@ def ncu_traffic():
             if line.startswith("kernel="):
                 kv = dict(t.split("=", 1) for t in line.split())
                 out[kv["kernel"]] = float(kv["dram_bytes_per_point"])
-                for key in ("fp64_pipe_active", "tensor_pipe_active"):
+                for key in ("fp64_pipe_active", "tensor_pipe_active", "fp64_inst_per_point"):
                     if key in kv:
                         pipe.setdefault(kv["kernel"], {})[key + "_ncu"] = float(kv[key])
     return out, pipe
@@ -571,8 +571,16 @@ def main():
                 out[k] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                           "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
                 out[k]["frac"] = out[k]["achieved"] / peaks["hbm_gbs"]
-                # what actually bounds it on GB300: FP64 issue (the FP64-pipe activity ncu measured)
+                # what actually bounds it on GB300: FP64 issue (the FP64-pipe activity ncu measured).
+                # fp64_issue: FP64 thread instructions (ncu count per point) per second against the
+                # live-measured FP64 rate taken as one instruction per two flops
                 out[k].update(fp64_pipe.get(k, {}))
+                ipp = out[k].pop("fp64_inst_per_point_ncu", None)
+                if ipp:
+                    ach = ipp * P / (ms * 1e-3) / 1e9
+                    pk = fp64_peak.value * 1e3 / 2.0
+                    out[k]["fp64_issue"] = {"achieved": ach, "peak": pk, "unit": "G FP64 thread-instructions/s",
+                                            "frac": ach / pk, "inst_per_point": ipp}
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
             if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]
