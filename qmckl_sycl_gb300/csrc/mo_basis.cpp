@@ -220,10 +220,11 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
   if (mo.provided && ctx->ao_basis.provided && ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE &&
       ctx->point.date > mo.mo_vgl_date && ctx->point.num >= 16384 && mo_vgl &&
       size_max >= 5 * ctx->point.num * mo.mo_num && ensure_device(ctx) && host_memory(mo_vgl)) {
-    // four chunks: measured on 40960 points (medium workload) 4.81 / 3.79 / 3.32 / 3.48 ms per
-    // step for 1 / 2 / 4 / 8 chunks (the ~193 GB/s device-to-host link needs 2.54 ms for the
-    // 491 MB of mo_vgl; smaller chunks lose more to kernel tails than they gain in overlap)
-    qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, 4);
+    // six chunks: measured on 40960 points (medium workload) 3.67 / 3.37 / 3.21 / 3.13 / 3.10 /
+    // 3.18 ms per step for 2 / 3 / 4 / 5 / 6 / 8 chunks (the ~193 GB/s device-to-host link needs
+    // 2.54 ms for the 491 MB of mo_vgl, the computation 1.83 ms; smaller chunks lose more to kernel
+    // tails than they gain in overlap)
+    qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, 6);
     if (rc != QMCKL_SUCCESS_DEVICE) return rc;
     mo.mo_vgl_date = ctx->date;
     return QMCKL_SUCCESS_DEVICE;

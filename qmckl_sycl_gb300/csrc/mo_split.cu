@@ -270,10 +270,33 @@ struct alignas(64) SplitJob {
 };
 
 
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bp = s - a;
-  e = (a - (s - bp)) + (b - bp);
+// Two FP32 values in one 64-bit register (column 2i in the low half, 2i + 1 in the high half) for
+// the packed FP32x2 instructions: two columns per instruction, each lane rounded exactly as the
+// scalar instruction would round it.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pack2(uint32_t lo, uint32_t hi) {
+  f32x2 d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "r"(lo), "r"(hi));
+  return d;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ float lo_f(f32x2 v) { return __uint_as_float((uint32_t)v); }
+__device__ __forceinline__ float hi_f(f32x2 v) { return __uint_as_float((uint32_t)(v >> 32)); }
+
+// Knuth's TwoSum on two columns at once: s = fl(a + b) and the exact rounding error e.
+__device__ __forceinline__ void two_sum2(f32x2 a, f32x2 b, f32x2& s, f32x2& e) {
+  s = add2(a, b);
+  const f32x2 bp = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bp)), sub2(b, bp));
 }
 
 // One 32-byte store (four doubles) to a 32-byte aligned global address.
@@ -403,7 +426,8 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, bool full16, uint32
 // rows x 64 contiguous bytes). it: the running fold-group index (advanced). Returns false when a
 // wait gave up.
 __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job, const TileRef& tr, uint32_t& it) {
-  float rhi[kHalfN], rlo[kHalfN];
+  // running two-sum of the main product, two columns per register: hi in h2, lo in l2
+  f32x2 h2[kHalfN / 2], l2[kHalfN / 2];
   const int nh = job.n_tile >> 1;             // columns of this warp: [hc, hc + nh)
   const uint32_t hc = (uint32_t)(f.half * nh);
   // Output row of this thread's tile row (lane = row), looked up before the folds so that the
@@ -434,16 +458,18 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
         if (hb) tmem_ld_async(f.lb + mcol + (uint32_t)c0 + 16, fb, rv, 16);
         tmem_wait_ld32(rv);
 #pragma unroll
-        for (int q = 0; q < 32; ++q) {
+        for (int q = 0; q < 32; q += 2) {
           if (c0 + q < kHalfN && (q < 8 || (q < 16 && fa) || (q >= 16 && hb && (q < 24 || fb)))) {
+            const int i = (c0 + q) >> 1;
+            const f32x2 v = pack2(rv[q], rv[q + 1]);
             if (kb == 0) {
-              rhi[c0 + q] = __uint_as_float(rv[q]);
-              rlo[c0 + q] = 0.f;
+              h2[i] = v;
+              l2[i] = 0ull;
             } else {
-              float s2, e2;
-              two_sum(rhi[c0 + q], __uint_as_float(rv[q]), s2, e2);
-              rhi[c0 + q] = s2;
-              rlo[c0 + q] += e2;
+              f32x2 s2, e2;
+              two_sum2(h2[i], v, s2, e2);
+              h2[i] = s2;
+              l2[i] = add2(l2[i], e2);
             }
           }
         }
@@ -461,11 +487,12 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
       uint32_t rc[16];
       tmem_ld_cols(f.lb + hc + (uint32_t)c0, full16, rc);
 #pragma unroll
-      for (int q = 0; q < 16; ++q) {
+      for (int q = 0; q < 16; q += 2) {
         if (q < 8 || full16) {
-          float s2, e2;
-          two_sum(rhi[c0 + q], __uint_as_float(rc[q]), s2, e2);
-          rhi[c0 + q] = s2 + (rlo[c0 + q] + e2);  // hi + (lo + e) rounded once to FP32 (2^-24 relative)
+          const int i = (c0 + q) >> 1;
+          f32x2 s2, e2;
+          two_sum2(h2[i], pack2(rc[q], rc[q + 1]), s2, e2);
+          h2[i] = add2(s2, add2(l2[i], e2));  // hi + (lo + e) rounded once to FP32 (2^-24 relative)
         }
       }
     }
@@ -485,12 +512,12 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
 #pragma unroll
       for (int c0 = 0; c0 < kHalfN; c0 += 4) {
         if (c0 + 4 <= ncol) {
-          st_global_v4(p + c0, f32_to_f64_int(rhi[c0]), f32_to_f64_int(rhi[c0 + 1]), f32_to_f64_int(rhi[c0 + 2]),
-                       f32_to_f64_int(rhi[c0 + 3]));
+          st_global_v4(p + c0, f32_to_f64_int(lo_f(h2[c0 >> 1])), f32_to_f64_int(hi_f(h2[c0 >> 1])),
+                       f32_to_f64_int(lo_f(h2[(c0 >> 1) + 1])), f32_to_f64_int(hi_f(h2[(c0 >> 1) + 1])));
         } else if (c0 < ncol) {
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            if (c0 + j < ncol) p[c0 + j] = f32_to_f64_int(rhi[c0 + j]);
+            if (c0 + j < ncol) p[c0 + j] = f32_to_f64_int(j & 1 ? hi_f(h2[(c0 + j) >> 1]) : lo_f(h2[(c0 + j) >> 1]));
         }
       }
     }
@@ -510,7 +537,7 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
   for (int c0 = 0; c0 < kHalfN; c0 += 8) {
     if (c0 < ncol) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) tb[f.lane * kTPitch + j] = rhi[c0 + j];
+      for (int j = 0; j < 8; ++j) tb[f.lane * kTPitch + j] = j & 1 ? hi_f(h2[(c0 + j) >> 1]) : lo_f(h2[(c0 + j) >> 1]);
       __syncwarp();
       const bool col_ok = c0 + cc < ncol;
 #pragma unroll
