@@ -105,6 +105,22 @@ __device__ __forceinline__ double f32_to_f64_int(float f) {
   return __longlong_as_double((long long)(sign | bits));
 }
 
+// The same for normal numbers and zeros only, in six integer instructions: the double's upper word
+// is the float's with the exponent re-biased (+896) and the mantissa shifted right by 3, its lower
+// word the mantissa's last 3 bits. f32_special() tells which inputs need f32_to_f64_int instead.
+__device__ __forceinline__ double f32_to_f64_normal(float f) {
+  const unsigned int u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+  const unsigned int hi = (u & 0x80000000u) | (a == 0 ? 0u : (a >> 3) + 0x38000000u);
+  double d;
+  asm("mov.b64 %0, {%1, %2};" : "=d"(d) : "r"(a << 29), "r"(hi));
+  return d;
+}
+// Subnormal, infinite or NaN.
+__device__ __forceinline__ bool f32_special(float f) {
+  const unsigned int a = __float_as_uint(f) & 0x7FFFFFFFu;
+  return a != 0 && a - 0x00800000u >= 0x7F000000u;
+}
+
 __device__ __forceinline__ void split3(double a, __nv_bfloat16& hi, __nv_bfloat16& mid, __nv_bfloat16& lo) {
   const float f = f64_to_f32_int(a);
   hi = __float2bfloat16_rn(f);
@@ -512,8 +528,13 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
 #pragma unroll
       for (int c0 = 0; c0 < kHalfN; c0 += 4) {
         if (c0 + 4 <= ncol) {
-          st_global_v4(p + c0, f32_to_f64_int(lo_f(h2[c0 >> 1])), f32_to_f64_int(hi_f(h2[c0 >> 1])),
-                       f32_to_f64_int(lo_f(h2[(c0 >> 1) + 1])), f32_to_f64_int(hi_f(h2[(c0 >> 1) + 1])));
+          const float v0 = lo_f(h2[c0 >> 1]), v1 = hi_f(h2[c0 >> 1]), v2 = lo_f(h2[(c0 >> 1) + 1]),
+                      v3 = hi_f(h2[(c0 >> 1) + 1]);
+          if (f32_special(v0) || f32_special(v1) || f32_special(v2) || f32_special(v3))
+            st_global_v4(p + c0, f32_to_f64_int(v0), f32_to_f64_int(v1), f32_to_f64_int(v2), f32_to_f64_int(v3));
+          else
+            st_global_v4(p + c0, f32_to_f64_normal(v0), f32_to_f64_normal(v1), f32_to_f64_normal(v2),
+                         f32_to_f64_normal(v3));
         } else if (c0 < ncol) {
 #pragma unroll
           for (int j = 0; j < 4; ++j)

@@ -113,3 +113,22 @@ def test_host_getter_overlaps_copies_bitwise():
     idx = np.arange(0, P, 97)
     ref = oracle.forward(s.with_points(s.coord[idx]), want=("mo_vgl",))["mo_vgl"]
     assert normwise_rel_err(host[idx], ref) <= MIXED_RTOL
+
+
+def test_split_zero_and_tiny_mo_columns():
+    # an MO whose coefficients are all zero gives exact zeros (the epilogue's float-to-double
+    # conversion of zeros), an MO scaled by 1e-20 keeps its own relative accuracy (the BF16 terms
+    # carry FP32's exponent range), and a 17-column tail checks the ragged last tile
+    s = config_small(3, point_num=300)
+    c = s.mo_coef.copy()
+    c[0] = 0.0
+    c[1] *= 1e-20
+    c[2] *= -3e12
+    s = _replace(s, mo_coef=np.ascontiguousarray(c))
+    ref = oracle.forward(s, want=("mo_vgl",))["mo_vgl"]
+    got = run(s, PRECISION_SPLIT_BF16)["mo_vgl"]
+    assert np.all(ref[:, :, 0] == 0.0)
+    assert np.array_equal(got[:, :, 0], np.zeros_like(got[:, :, 0]))
+    for m in (1, 2, 3):
+        for comp in range(5):
+            assert normwise_rel_err(got[:, comp, m], ref[:, comp, m]) <= MIXED_RTOL, (m, comp)
