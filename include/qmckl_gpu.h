@@ -480,7 +480,7 @@ qmckl_exit_code_device qmckl_batch_touch_device(qmckl_batch_device batch);
  * variable QMCKL_GB300_TUNE_CACHE names a file, in that file):
  *   params[0] nucleus-chunk level of the AO kernel's warp tasks (0 = whole molecule, v ~ 2^v chunks)
  *   params[1] FP64 contraction CTA tile: 0 = 64x64, 1 = 128x64, 2 = 64x128
- *   params[2] split-BF16 contraction: widest column tile (16..96, multiple of 16)
+ *   params[2] split-BF16 contraction: widest column tile (16..160, multiple of 16)
  * set pins the parameters (n = 3; no autotuning afterwards); get reads them (-1 = not chosen yet);
  * autotune re-times the candidates now (members must be ready to provide). */
 qmckl_exit_code_device qmckl_batch_set_tuning_device(qmckl_batch_device batch, const int32_t* params, int64_t n);

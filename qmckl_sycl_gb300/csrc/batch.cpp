@@ -465,7 +465,7 @@ qmckl_exit_code_device autotune(Batch* b, const std::vector<Member>& ms) {
   for (const Member& e : ms) max_level = std::max(max_level, ao_level_count(e.ctx->ao_basis.tables) - 1);
   b->tune.v[0] = 0;
   b->tune.v[1] = 0;
-  b->tune.v[2] = 96;
+  b->tune.v[2] = 160;
   qmckl_exit_code_device rc = build_descriptors(b, ms);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
   stage_order(b, b->members[0]->stream);
@@ -514,7 +514,7 @@ qmckl_exit_code_device autotune(Batch* b, const std::vector<Member>& ms) {
     b->tune.v[1] = best_shape;
   }
   if (split && b->tune.v[1] < 0) b->tune.v[1] = 0;
-  if (!split) b->tune.v[2] = 96;
+  if (!split) b->tune.v[2] = 160;
   drop_graph(b);
   b->sig.clear();
   return QMCKL_SUCCESS_DEVICE;
@@ -622,7 +622,7 @@ qmckl_exit_code_device qmckl_batch_set_tuning_device(qmckl_batch_device batch, c
   if (!params) return fail(b->handles[0], QMCKL_INVALID_ARG_2_DEVICE, fn, "NULL pointer");
   if (n != 3) return fail(b->handles[0], QMCKL_INVALID_ARG_3_DEVICE, fn, "expected 3 parameters");
   if (params[0] < 0 || params[0] > 30 || params[1] < 0 || params[1] >= kGemmShapes || params[2] < 16 ||
-      params[2] > 96 || params[2] % 16 != 0)
+      params[2] > 160 || params[2] % 16 != 0)
     return fail(b->handles[0], QMCKL_INVALID_ARG_2_DEVICE, fn, "parameter out of range");
   for (int i = 0; i < 3; ++i) b->tune.v[i] = params[i];
   b->pinned = true;

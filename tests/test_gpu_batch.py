@@ -52,7 +52,7 @@ def test_batch_matches_single_context_and_oracle(mode):
         b.set_precision(mode)
         outs = b.get_mo_vgl()
         tune = b.tuning()
-        assert tune[0] >= 0 and tune[1] in (0, 1, 2) and 16 <= tune[2] <= 96
+        assert tune[0] >= 0 and tune[1] in (0, 1, 2) and 16 <= tune[2] <= 160
         assert b.launch_count() == 5
         for s, got in zip(systems, outs):
             assert np.array_equal(got, single(s, mode)), s.name
@@ -72,7 +72,7 @@ def test_every_tuning_gives_the_same_bits(mode):
     try:
         b.set_precision(mode)
         first = None
-        configs = [(0, 0, 96), (1, 1, 64), (2, 2, 48), (3, 0, 32), (30, 1, 16)]
+        configs = [(0, 0, 160), (1, 1, 128), (2, 2, 96), (3, 0, 48), (30, 1, 16)]
         for params in configs:
             b.set_tuning(params)
             assert b.tuning() == params
@@ -136,7 +136,7 @@ def test_autotune_and_async():
         b.set_precision(PRECISION_SPLIT_BF16)
         b.autotune()
         t = b.tuning()
-        assert t[0] >= 0 and 16 <= t[2] <= 96
+        assert t[0] >= 0 and 16 <= t[2] <= 160
         b.set_async(True)
         b.touch()
         b.provide_mo_vgl()
