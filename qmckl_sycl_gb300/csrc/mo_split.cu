@@ -29,10 +29,11 @@
 // 128B-swizzled shared-memory buffers; warp 1 owns tensor memory and issues the MMAs (24 per K
 // block: six products x four K=16 steps); eight fold warps, two per 32-lane quarter of tensor
 // memory (one row per thread, one column half per warp), fold the main product and write the
-// tile's FP64 results through a small per-warp transposition buffer, so that each store
-// instruction covers four 64-byte row segments. An MMA costs nearly the same time for N = 32
-// to 128 (its A operand fetch dominates), so the widest tile that tensor memory and shared
-// memory allow sets the rate: 160 columns halve the MMA count of 80-column tiles. Every
+// tile's FP64 results from registers (32-byte stores of each thread's row segment, or, for rows
+// not 32-byte aligned, through a small per-warp transposition buffer). An MMA costs nearly the
+// same time for N = 32 to 160 (its A operand fetch dominates), so the widest tile that tensor
+// memory and shared memory allow sets the rate: 160 columns halve the MMA count of 80-column
+// tiles. Every
 // mbarrier wait is bounded (~1 s); on expiry the kernel records an error code, drains what it
 // issued, releases its tensor memory and exits, and the host reports QMCKL_FAILURE_DEVICE.
 #include <cuda.h>
