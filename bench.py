@@ -47,6 +47,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=8.0, help="wall budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the batched-form measurement")
+    p.add_argument("--long-steps", type=int, default=200,
+                   help="steps of the headline form's second, longer timed region (0: skip it)")
     p.add_argument("--batch-molecules", type=int, default=64, help="molecules of the batched workload")
     p.add_argument("--batch-walkers", type=int, default=32, help="walkers per molecule of the batched workload")
     return p.parse_args()
@@ -88,6 +90,81 @@ class Dist:
         t = torch.tensor([float(x)], dtype=torch.float64)
         self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
         return float(t.item())
+
+
+class NvmlSampler:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, read-only queries) every
+    2 ms on a host thread during a timed region: the timed regions here last tens of
+    milliseconds, shorter than nvidia-smi's sampling period."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, gpu, period=0.002):
+        self.gpu, self.period = gpu, period
+        self.samples, self.reasons, self.max_mhz = [], set(), None
+        self.ok = False
+        try:
+            self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if self.nv.nvmlInit_v2() != 0:
+                return
+            self.h = ctypes.c_void_p()
+            if self.nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu), ctypes.byref(self.h)) != 0:
+                return
+            m = ctypes.c_uint()
+            if self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(m)) == 0:
+                self.max_mhz = float(m.value)
+            self.reason_fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(self.nv, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            self.ok = True
+        except (OSError, AttributeError):
+            self.ok = False
+
+    def _run(self):
+        mhz, r = ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(mhz)) == 0:
+                self.samples.append(float(mhz.value))
+            if self.reason_fn(self.h, ctypes.byref(r)) == 0:
+                for bit, name in self.REASONS.items():
+                    if r.value & bit:
+                        self.reasons.add(name)
+            time.sleep(self.period)
+
+    def __enter__(self):
+        if self.ok:
+            self.stop = False
+            self.t = threading.Thread(target=self._run, daemon=True)
+            self.t.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self.ok:
+            self.stop = True
+            self.t.join()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "samples": 0,
+                    "source": "nvml"}
+        return {"sm_mhz": statistics.median(self.samples), "sm_max_mhz": self.max_mhz,
+                "reasons": sorted(self.reasons), "samples": len(self.samples), "source": "nvml, every 2 ms"}
+
+
+def clock_sampler(gpu):
+    s = NvmlSampler(gpu)
+    return s if s.ok else ClockSampler(gpu)
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
 
 
 class ClockSampler:
@@ -177,26 +254,23 @@ def ncu_traffic():
 
 
 def cpu_baseline(s, seconds, threads=None):
-    """The reference algorithm (oracle port, all host threads) on samples of the same
-    workload until `seconds` of wall time: returns points/s and the sample description."""
+    """The reference algorithm (oracle port, all host threads) on the whole workload, repeated
+    until `seconds` of wall time (at least once): returns points/s, threads and the sample, and
+    the last result (the oracle's mo_vgl of the workload)."""
     from oracle import oracle
 
     L = oracle.lib()
     if threads:
         L.oracle_set_num_threads(threads)
     nthreads = L.oracle_num_threads()
-    n = min(s.point_num, max(256, 64 * nthreads))
-    rng = np.random.default_rng(7)
-    done, t_total, reps = 0, 0.0, 0
-    while t_total < seconds and reps < 50:
-        idx = rng.choice(s.point_num, size=n, replace=False)
-        sub = s.with_points(s.coord[np.sort(idx)])
+    t_total, reps, out = 0.0, 0, None
+    while reps == 0 or (t_total < seconds and reps < 20):
         t0 = time.perf_counter()
-        oracle.forward(sub, want=("mo_vgl",))
+        out = oracle.forward(s, want=("mo_vgl",))["mo_vgl"]
         t_total += time.perf_counter() - t0
-        done += n
         reps += 1
-    return done / t_total, nthreads, "%d samples x %d points of the workload, %.1f s wall" % (reps, n, t_total)
+    return (s.point_num * reps / t_total, nthreads,
+            "the whole workload (%d points) x %d, %.1f s wall" % (s.point_num, reps, t_total), out)
 
 
 def run_reference(args, dist):
@@ -209,31 +283,33 @@ def run_reference(args, dist):
 
     nthreads = oracle.lib().oracle_num_threads()
     times = []
-    n = min(s.point_num, max(256, 64 * nthreads))
-    rng = np.random.default_rng(11)
+    # one step = the whole workload (every point), as the GPU arm's step
     for i in range(args.warmup + args.steps):
-        sub = s.with_points(s.coord[np.sort(rng.choice(s.point_num, size=n, replace=False))])
         t0 = time.perf_counter()
-        oracle.forward(sub, want=("mo_vgl",))
+        oracle.forward(s, want=("mo_vgl",))
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(dt)
-    v = n * len(times) / sum(times)
+    v = s.point_num * len(times) / sum(times)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": config_dict(s, "reference CPU path (oracle port of src/qmckl_ao_sycl.cpp + src/qmckl_mo_sycl.cpp)"),
-        "cpu_baseline": {"value": v, "unit": "points/s", "cores": nthreads, "kind": "port",
-                         "sample": "%d random points of the workload per step" % n},
+        "config": config_dict(s), "form": REF_FORM,
+        "cpu_baseline": {"value": v, "unit": "points/s", "cores": nthreads, "cpu": cpu_model(), "kind": "port",
+                         "sample": "the whole workload (%d points) per step" % s.point_num},
         "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def config_dict(s, form):
-    return {"workload": "medium: %d nuclei, %d shells, %d primitives, %d AOs, %d MOs, %d points (%s)" % (
-        s.nucl_num, s.shell_num, s.prim_num, s.ao_num, s.mo_num, s.point_num, form),
+# what the reference arm runs (the same workload and config as this arm's)
+REF_FORM = "reference CPU path: the oracle port of src/qmckl_ao_sycl.cpp + src/qmckl_mo_sycl.cpp, FP64, all host threads"
+
+
+def config_dict(s):
+    return {"workload": "medium: %d nuclei, %d shells, %d primitives, %d AOs, %d MOs, %d points" % (
+        s.nucl_num, s.shell_num, s.prim_num, s.ao_num, s.mo_num, s.point_num),
             "nucl_num": s.nucl_num, "shell_num": s.shell_num, "prim_num": s.prim_num, "ao_num": s.ao_num,
             "mo_num": s.mo_num, "point_num": s.point_num, "seed": 0,
             "l2": "no flush: per-step working set %.2f GB (ao_vgl + mo_vgl) > 129 MB L2" % (
@@ -298,7 +374,7 @@ def time_e2e(ctx, s, steps, warmup):
     return dt, coord.nbytes, out.nbytes, out
 
 
-def time_batched(dist, steps, warmup, peaks, fp64_peak, molecules=64, walkers=32):
+def time_batched(dist, steps, warmup, peaks, fp64_peak, molecules=64, walkers=32, with_oracle=False):
     """The batched form on the 64-molecule workload: every member's MO vgl per step through
     qmckl_batch_provide_mo_vgl_device (graph replay, autotuned), both precision forms, plus
     one profiled pass with ordinary launches for the per-stage times."""
@@ -374,10 +450,21 @@ def time_batched(dist, steps, warmup, peaks, fp64_peak, molecules=64, walkers=32
             ref = [c.get_mo_vgl(sy.point_num) for c, sy in zip(ctxs, systems)]
         else:
             worst = np.zeros(5)
+            worst_o = {"fp64": np.zeros(5), "mixed": np.zeros(5)}
             for c, sy, r in zip(ctxs, systems, ref):
                 g = c.get_mo_vgl(sy.point_num)
                 worst = np.maximum(worst, np.abs(g - r).max(axis=(0, 2)) / np.abs(r).max(axis=(0, 2)))
+                if with_oracle:
+                    from oracle import oracle
+
+                    o = oracle.forward(sy, want=("mo_vgl",))["mo_vgl"]
+                    sc = np.abs(o).max(axis=(0, 2))
+                    worst_o["fp64"] = np.maximum(worst_o["fp64"], np.abs(r - o).max(axis=(0, 2)) / sc)
+                    worst_o["mixed"] = np.maximum(worst_o["mixed"], np.abs(g - o).max(axis=(0, 2)) / sc)
             out["mixed_vs_fp64_error"] = {"max_rel_normwise_over_molecules": [float(x) for x in worst]}
+            if with_oracle:
+                out["error_vs_oracle"] = {f: {"max_rel_normwise_over_molecules": [float(x) for x in w]}
+                                          for f, w in worst_o.items()}
     out["mixed_over_fp64"] = out["forms"]["mixed"]["value"] / out["forms"]["fp64"]["value"]
     b.close()
     for c in ctxs:
@@ -529,7 +616,7 @@ def main():
     headline = args.form or ("mixed" if "mixed" in forms else "fp64")
 
     results = {}
-    samplers = {f: ClockSampler(dist.local_rank) for f in forms}
+    samplers = {f: clock_sampler(dist.local_rank) for f in forms}
     clocks = samplers[headline]
     for form in forms:
         # the FP64 form (150 ms a step) is timed on at most 10 steps when it is not the headline
@@ -539,8 +626,35 @@ def main():
         total_points = dist.sum(P * k)
         results[form] = dict(ms=t, value=total_points / (t * 1e-3), stats=stats, launches=launches, steps=k)
 
-    # accuracy of the mixed form against the FP64 form on the same inputs
-    acc = None
+    # the headline form once more over a longer timed region (at least 200 steps), with its own
+    # clock record: the timed region of K steps lasts only tens of milliseconds
+    long_run = None
+    if args.long_steps > 0:
+        long_k = max(args.long_steps, args.steps)
+        long_clocks = clock_sampler(dist.local_rank)
+        ms_long, _, _ = time_form(ctx, s, headline, long_k, args.warmup, dist, long_clocks)
+        t_long = dist.max(ms_long)
+        long_run = {"steps": long_k, "value": dist.sum(P * long_k) / (t_long * 1e-3),
+                    "ms_per_step": t_long / long_k, "clocks": long_clocks.summary()}
+
+    # CPU baseline: the oracle port on the whole workload (rank 0, one GPU), whose result is also
+    # the reference for the error of both forms below
+    cpu, oracle_mo = None, None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        v, cores, sample, oracle_mo = cpu_baseline(s, args.cpu_seconds)
+        cpu = {"value": v, "unit": "points/s", "cores": cores, "cpu": cpu_model(), "kind": "port", "sample": sample}
+
+    def errors(got, ref):
+        scale = np.abs(ref).max(axis=(0, 2))
+        diff = np.abs(got - ref)
+        big = np.abs(ref) >= 1e-3 * scale[None, :, None]  # elementwise relative error where |ref| is not tiny
+        rel = np.where(big, diff / np.where(big, np.abs(ref), 1.0), 0.0)
+        return {"max_abs": [float(x) for x in diff.max(axis=(0, 2))],
+                "max_rel_normwise": [float(x) for x in diff.max(axis=(0, 2)) / scale],
+                "max_rel_elementwise_where_ref_ge_1e-3_max": [float(x) for x in rel.max(axis=(0, 2))]}
+
+    # accuracy of the mixed form against the FP64 form and against the oracle, on the same inputs
+    acc = acc_oracle = None
     if "mixed" in forms:
         ctx.set_precision(0)
         ctx.touch()
@@ -548,9 +662,10 @@ def main():
         ctx.set_precision(1)
         ctx.touch()
         got = ctx.get_mo_vgl(P)
-        scale = np.abs(ref).max(axis=(0, 2))
-        acc = {"max_abs": [float(x) for x in np.abs(got - ref).max(axis=(0, 2))],
-               "max_rel_normwise": [float(x) for x in np.abs(got - ref).max(axis=(0, 2)) / scale]}
+        acc = errors(got, ref)
+        if oracle_mo is not None:
+            acc_oracle = {"mixed": errors(got, oracle_mo), "fp64": errors(ref, oracle_mo),
+                          "points": P, "components": ["value", "d/dx", "d/dy", "d/dz", "laplacian"]}
         del ref, got
 
     # end to end through the C ABI with host buffers (headline form), as a caller runs it: without
@@ -565,25 +680,25 @@ def main():
     def roof(form):
         st = results[form]["stats"]
         out = {}
-        # AO kernel: FP64 ao_vgl (8 bytes per element) or the three BF16 planes (6 bytes)
-        for k, per_elem in (("ao_vgl_fused", 8.0), ("ao_vgl_fused_bf16_planes", 6.0)):
+        # AO kernel: algorithmic bytes 8 (5A + 3) per point (the FP64 ao_vgl written, coordinates
+        # read) for both forms; the split-BF16 form's kernel writes three BF16 planes instead (6
+        # bytes per element), reported beside it
+        for k in ("ao_vgl_fused", "ao_vgl_fused_bf16_planes"):
             if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]
                 ms = tot / max(n, 1)
-                alg = (per_elem * 5 * A + 24.0) * P
+                alg = (8.0 * 5 * A + 24.0) * P
                 out[k] = {"bound": "hbm", "achieved": alg / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
-                          "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None}
+                          "unit": "GB/s", "ms_per_launch": ms, "traffic": traffic.get(k, 0) * P or None,
+                          "algorithmic_bytes": alg}
                 out[k]["frac"] = out[k]["achieved"] / peaks["hbm_gbs"]
-                # what actually bounds it on GB300: FP64 issue (the FP64-pipe activity ncu measured).
-                # fp64_issue: FP64 thread instructions (ncu count per point) per second against the
-                # live-measured FP64 rate taken as one instruction per two flops
-                out[k].update(fp64_pipe.get(k, {}))
-                ipp = out[k].pop("fp64_inst_per_point_ncu", None)
-                if ipp:
-                    ach = ipp * P / (ms * 1e-3) / 1e9
-                    pk = fp64_peak.value * 1e3 / 2.0
-                    out[k]["fp64_issue"] = {"achieved": ach, "peak": pk, "unit": "G FP64 thread-instructions/s",
-                                            "frac": ach / pk, "inst_per_point": ipp}
+                if k == "ao_vgl_fused_bf16_planes":
+                    written = (6.0 * 5 * A + 24.0) * P
+                    out[k]["planes_bytes"] = written
+                    out[k]["planes_frac"] = written / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]
+                # what bounds it on GB300 is the latency of its FP64 chains, not HBM: the FP64-pipe
+                # activity ncu measured on the same kernel
+                out[k].update({kk: v for kk, v in fp64_pipe.get(k, {}).items() if kk != "fp64_inst_per_point_ncu"})
         for k in ("mo_vgl_dgemm", "mo_vgl_split_bf16"):
             if st.get(k, (0, 0))[0] > 0:
                 n, tot = st[k]
@@ -609,17 +724,12 @@ def main():
     roofline["peak_source"] = ("live DMMA m16n8k4 f64 probe (MEASURED_PEAKS.json has no FP64 figure)"
                                if dom == "mo_vgl_dgemm" else "%s MEASURED_PEAKS.json" % peak_src)
 
-    cpu = None
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        v, cores, sample = cpu_baseline(s, args.cpu_seconds)
-        cpu = {"value": v, "unit": "points/s", "cores": cores, "kind": "port", "sample": sample}
-
     adj = time_adjoint(dist, args.steps, args.warmup, fp64_peak.value)
     shared = time_shared_exponentials(dist, args.steps, args.warmup)
     bt = None
     if not args.no_batched:
         bt = time_batched(dist, args.steps, args.warmup, peaks, fp64_peak.value, args.batch_molecules,
-                          args.batch_walkers)
+                          args.batch_walkers, with_oracle=dist.rank == 0 and not args.no_cpu_baseline)
         bt["mixed_over_plain_fp64_medium"] = bt["forms"]["mixed"]["value"] / results["fp64"]["value"]
     if dist.rank != 0:
         return
@@ -629,17 +739,19 @@ def main():
         "warmup": args.warmup, "ms_per_step": hr["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if headline == "fp64" else "f64+bf16x3",
         "data": "synthetic (seeded generator with the medium configuration's shapes and distributions)",
-        "config": config_dict(s, "%s form" % headline),
+        "config": config_dict(s), "form": "split-BF16 (mixed)" if headline == "mixed" else "FP64 (plain)",
         "roofline": roofline, "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "points/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": hr["launches"], "clocks": clocks.summary(),
         "clocks_by_form": {f: samplers[f].summary() for f in forms},
         "forms": {f: {"value": results[f]["value"], "ms_per_step": results[f]["ms"] / results[f]["steps"],
                       "steps": results[f]["steps"], "kernels": rf[f]} for f in forms},
-        "fp64_peak_tflops": fp64_peak.value,
+        "fp64_peak_tflops": fp64_peak.value, "long_run": long_run,
     }
     if acc:
         line["mixed_vs_fp64_error"] = acc
+    if acc_oracle:
+        line["error_vs_oracle"] = acc_oracle
         line["mixed_over_fp64"] = results["mixed"]["value"] / results["fp64"]["value"]
     line["adjoint"] = adj
     line["shared_exponentials"] = shared

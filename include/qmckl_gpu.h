@@ -407,8 +407,9 @@ qmckl_exit_code_device qmckl_prim_value_check_device(qmckl_context_device contex
  * QMCKL_FAILURE_DEVICE.
  *
  * The first call on a device resolves the array's device address for that device (with that
- * device current); make that first call before any stream capture. All calls share the one
- * array, so calls whose work overlaps on the GPU (different streams, or concurrent host
+ * device current); make that first call before any stream capture. Every call waits for
+ * cuda_stream before it returns (it reads the kernel's error word on the host). All calls share
+ * the one array, so calls whose work overlaps on the GPU (different streams, or concurrent host
  * threads) race on it: serialise them. */
 qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(const double* ao, int64_t rows, int64_t ao_num,
                                                                    const double* coefficient, int64_t mo_num,
@@ -516,6 +517,32 @@ qmckl_exit_code_device qmckl_vjp_ao_vgl_device(qmckl_context_device context, con
 /* Test hook for allocation failure handling: the n-th device allocation from now on
  * (n >= 1) fails as if cudaMalloc had failed; n = 0 disables the hook. */
 qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device context, int64_t n);
+
+/* Test hook for the device-side failure path of the split-BF16 contraction (no counterpart in the
+ * reference, whose only failure handling is error codes, src/qmckl_basic_functions.cpp:51): every
+ * mbarrier wait of that kernel gives up after wait_cycles clock cycles (0 restores the default,
+ * about one second), and with withhold_loads = 1 its producer issues no operand loads, so the first
+ * wait of its consumers is one that nothing completes. On expiry the kernel records an error word,
+ * releases its tensor memory and exits; the call returns QMCKL_FAILURE_DEVICE and the context
+ * stays usable. Bad wait_cycles (< 0): QMCKL_INVALID_ARG_2_DEVICE; withhold_loads not 0 or 1:
+ * QMCKL_INVALID_ARG_3_DEVICE. */
+qmckl_exit_code_device qmckl_set_split_wait_test_device(qmckl_context_device context, int64_t wait_cycles,
+                                                        int32_t withhold_loads);
+
+/* Debug build with bounds checks (no counterpart in the reference). The library built with
+ * -DQMCKL_BOUNDS_CHECK (python -m qmckl_sycl_gb300.build --bounds: _lib/libqmckl_gpu_bounds.so)
+ * tests the element index of the kernels' global stores against the extent of the array they
+ * write; an out-of-range store is skipped and the first one recorded. This returns 1 and fills
+ * site (the store site: 1 AO rows, 2 AO planes, 3 shell_vgl, 4 point order, 5 split-BF16 output,
+ * 6 split planes, 7 FP64 contraction output, 8 split-K sums, 9 distances, 10 transposes and
+ * copies, 11 adjoint), index and extent (elements) when a store was out of range on the current
+ * device, 0 when none was, -1 for the normal build (no checks) and -2 on a CUDA error; reset = 1
+ * clears the records. Any pointer may be NULL. */
+int32_t qmckl_bounds_check_status_device(int32_t reset, int64_t* site, int64_t* index, int64_t* extent);
+/* Self-test of that recording: a one-thread kernel evaluates the check for element `index` of an
+ * array of `extent` elements (site 10) and stores nothing. Returns 0 when it ran, -1 for the normal
+ * build, -2 on a CUDA error. */
+int32_t qmckl_bounds_check_selftest_device(int64_t index, int64_t extent);
 
 /* Library build information: "sm_103a" plus the git-independent build flags. */
 const char* qmckl_gb300_build_info(void);

@@ -13,8 +13,22 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+ASAN_LIB_PATH = os.path.join(HERE, "_build", "liboracle_asan.so")
 REF_PATH = os.path.join(HERE, "_ref", "libqmckl_ref.so")
-REFERENCE_DIR = "/root/reference"
+
+
+def reference_dir():
+    """The reference checkout's location (QMCKL_REFERENCE_DIR, else the default of the recipe
+    oracle/Makefile.ref), or None when no checkout is there."""
+    d = os.environ.get("QMCKL_REFERENCE_DIR")
+    if not d:
+        try:
+            d = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "print-reference"],
+                               capture_output=True, text=True, timeout=30).stdout.strip()
+        except (OSError, subprocess.SubprocessError):
+            d = ""
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
+
 
 _f64 = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _i64 = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
@@ -23,26 +37,31 @@ _vp = ctypes.c_void_p
 _I = ctypes.c_int64
 
 
-def build_oracle(force=False):
-    """Compiles qmckl_oracle.c (no FP contraction, OpenMP) into _build/liboracle.so."""
+def build_oracle(force=False, sanitize=False):
+    """Compiles qmckl_oracle.c (no FP contraction, OpenMP) into _build/liboracle.so, or with
+    AddressSanitizer and UndefinedBehaviorSanitizer into _build/liboracle_asan.so (sanitize)."""
     src = os.path.join(HERE, "qmckl_oracle.c")
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
-        return LIB_PATH
-    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    tmp = LIB_PATH + ".tmp%d" % os.getpid()
+    out = ASAN_LIB_PATH if sanitize else LIB_PATH
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(src):
+        return out
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    tmp = out + ".tmp%d" % os.getpid()
+    extra = ["-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-fno-omit-frame-pointer", "-g"] \
+        if sanitize else []
     subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-                           "-std=c11", src, "-o", tmp, "-lm"])
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+                           "-std=c11"] + extra + [src, "-o", tmp, "-lm"])
+    os.replace(tmp, out)
+    return out
 
 
-def build_reference(reference_dir=REFERENCE_DIR):
+def build_reference(ref_dir=None):
     """Builds oracle/_ref/libqmckl_ref.so from the reference sources where they lie.
     Returns the path, or None when the reference checkout is not present."""
-    if not os.path.isdir(os.path.join(reference_dir, "src")):
+    ref = ref_dir or reference_dir()
+    if not ref or not os.path.isdir(os.path.join(ref, "src")):
         return None
     subprocess.check_call(["make", "-s", "-j8", "-f", os.path.join(HERE, "Makefile.ref"),
-                           "REFERENCE=" + reference_dir], cwd=os.path.dirname(HERE))
+                           "REFERENCE=" + ref], cwd=os.path.dirname(HERE))
     return REF_PATH
 
 
@@ -53,8 +72,8 @@ _ref = None
 def lib():
     global _lib
     if _lib is None:
-        build_oracle()
-        L = ctypes.CDLL(LIB_PATH)
+        # QMCKL_ORACLE_SANITIZE=1: the sanitizer build (the process must preload libasan)
+        L = ctypes.CDLL(build_oracle(sanitize=os.environ.get("QMCKL_ORACLE_SANITIZE") == "1"))
         L.oracle_num_threads.restype = ctypes.c_int
         L.oracle_set_num_threads.argtypes = [ctypes.c_int]
         L.oracle_forward.restype = ctypes.c_int

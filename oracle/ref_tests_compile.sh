@@ -10,9 +10,10 @@
 # would run on the host over device memory).
 #
 #   sh oracle/ref_tests_compile.sh [REFERENCE_DIR]
+# (default: QMCKL_REFERENCE_DIR, else the location oracle/Makefile.ref uses)
 set -e
-REF=${1:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-$(make -s -f "$HERE/Makefile.ref" print-reference)}
 REPO=$(dirname "$HERE")
 OUT=$HERE/_ref/compat
 LIB=$REPO/qmckl_sycl_gb300/_lib

@@ -5,7 +5,13 @@ and linked into one shared library exporting the C ABI of include/qmckl_gpu.h. H
 is compiled without floating-point contraction so that host-side table arithmetic rounds
 like the reference.
 
-    python -m qmckl_sycl_gb300.build [--force] [--verbose]
+    python -m qmckl_sycl_gb300.build [--force] [--verbose] [--bounds]
+
+--bounds builds the debug variant _lib/libqmckl_gpu_bounds.so instead (objects in _build_bounds/),
+compiled with -DQMCKL_BOUNDS_CHECK: every checked global store of the kernels tests its index
+against the array's extent and records the first violation (qmckl_bounds_check_status_device).
+--sanitize builds _lib/libqmckl_gpu_asan.so (objects in _build_asan/): host code with
+AddressSanitizer and UndefinedBehaviorSanitizer, for the CPU tests of the argument paths.
 """
 import os
 import subprocess
@@ -18,6 +24,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libqmckl_gpu.so")
+BOUNDS_LIB = os.path.join(LIBDIR, "libqmckl_gpu_bounds.so")
+ASAN_LIB = os.path.join(LIBDIR, "libqmckl_gpu_asan.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -47,13 +55,14 @@ def _headers_mtime():
     return m
 
 
-def _compile(src, verbose):
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def _compile(src, verbose, build_dir=BUILD, extra=(), arch=ARCH):
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _headers_mtime()):
         return obj
-    cmd = [nvcc()] + ARCH + COMMON + ["-c", src, "-o", obj]
+    flags = list(arch) + COMMON + list(extra)
+    cmd = [nvcc()] + flags + ["-c", src, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "cu"] + ARCH + COMMON + ["-c", src, "-o", obj]
+        cmd = [nvcc(), "-x", "cu"] + flags + ["-c", src, "-o", obj]
     if verbose:
         cmd += ["-Xptxas", "-v"]
         print(" ".join(cmd), flush=True)
@@ -65,27 +74,37 @@ def _compile(src, verbose):
     return obj
 
 
-def build(force=False, verbose=False, jobs=None):
-    os.makedirs(BUILD, exist_ok=True)
+# Host code under AddressSanitizer and UndefinedBehaviorSanitizer, for the CPU tests of the
+# C ABI's argument paths (device code as PTX only: that build never runs a kernel).
+SANITIZE = ["-Xcompiler", "-fsanitize=address,-fsanitize=undefined,-fno-sanitize-recover=all,-fno-omit-frame-pointer,-g"]
+
+
+def build(force=False, verbose=False, jobs=None, bounds=False, sanitize=False):
+    build_dir = BUILD + ("_bounds" if bounds else "_asan" if sanitize else "")
+    lib = BOUNDS_LIB if bounds else (ASAN_LIB if sanitize else LIB)
+    extra = ["-DQMCKL_BOUNDS_CHECK"] if bounds else (SANITIZE if sanitize else [])
+    arch = ["-gencode", "arch=compute_103a,code=compute_103a"] if sanitize else ARCH
+    os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sources()
     if force:
-        for f in os.listdir(BUILD):
+        for f in os.listdir(build_dir):
             if f.endswith(".o"):
-                os.remove(os.path.join(BUILD, f))
-    with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs)):
-        return LIB
-    tmp = LIB + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+                os.remove(os.path.join(build_dir, f))
+    with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose, build_dir, extra, arch), srcs))
+    if (not force and os.path.exists(lib)
+            and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs)):
+        return lib
+    tmp = lib + ".tmp%d" % os.getpid()
+    cmd = [nvcc()] + arch + (SANITIZE if sanitize else []) + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="--verbose" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="--verbose" in sys.argv, bounds="--bounds" in sys.argv,
+                sanitize="--sanitize" in sys.argv))

@@ -12,6 +12,20 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 HEADER = os.path.join(ROOT, "include", "qmckl_gpu.h")
 LIB_PATH = os.path.join(HERE, "_lib", "libqmckl_gpu.so")
+# the debug build with bounds checks on the kernels' stores (python -m qmckl_sycl_gb300.build --bounds)
+BOUNDS_LIB_PATH = os.path.join(HERE, "_lib", "libqmckl_gpu_bounds.so")
+# host code under AddressSanitizer/UndefinedBehaviorSanitizer (python -m qmckl_sycl_gb300.build --sanitize)
+ASAN_LIB_PATH = os.path.join(HERE, "_lib", "libqmckl_gpu_asan.so")
+
+
+def lib_path():
+    """The library this process loads: the bounds-checked build when QMCKL_GB300_BOUNDS_CHECK=1,
+    the sanitizer build when QMCKL_GB300_SANITIZE=1, else the normal one."""
+    if os.environ.get("QMCKL_GB300_BOUNDS_CHECK") == "1":
+        return BOUNDS_LIB_PATH
+    if os.environ.get("QMCKL_GB300_SANITIZE") == "1":
+        return ASAN_LIB_PATH
+    return LIB_PATH
 
 
 class MemoryInfo(ctypes.Structure):
@@ -96,11 +110,12 @@ def lib():
     """The loaded native library with every header prototype bound."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        path = lib_path()
+        if not os.path.exists(path):
             raise RuntimeError(
                 "qmckl_sycl_gb300 native library not found at %s; build it with "
-                "`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)" % LIB_PATH)
-        L = ctypes.CDLL(LIB_PATH)
+                "`python -c 'import __graft_entry__ as g; g.build()'` (there is no CPU fallback)" % path)
+        L = ctypes.CDLL(path)
         for name, (res, args) in parse_header().items():
             f = getattr(L, name)
             f.restype = res

@@ -543,6 +543,7 @@ extern "C" {
 
 // src/qmckl_ao_sycl.cpp:1067-1231, computed on the host with the same operations.
 qmckl_exit_code_device qmckl_finalize_ao_basis_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_finalize_ao_basis_device");
   Ctx* ctx = checked(context);
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, "qmckl_finalize_ao_basis_device", nullptr);
   int64_t N = 0;
@@ -981,6 +982,7 @@ qmckl_exit_code_device qmckl_get_ao_basis_coefficient_normalized_device(qmckl_co
 
 // ---------------------------------------------------------------- provides
 qmckl_exit_code_device qmckl_provide_ao_basis_shell_vgl_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_ao_basis_shell_vgl_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_provide_ao_basis_shell_vgl_device";
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
@@ -1021,6 +1023,7 @@ static qmckl_exit_code_device compute_ao_value(Ctx* ctx, qmckl_context_device co
 }
 
 qmckl_exit_code_device qmckl_provide_ao_basis_ao_vgl_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_ao_basis_ao_vgl_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_provide_ao_basis_ao_vgl_device";
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
@@ -1037,6 +1040,7 @@ qmckl_exit_code_device qmckl_provide_ao_basis_ao_vgl_device(qmckl_context_device
 }
 
 qmckl_exit_code_device qmckl_provide_ao_basis_ao_value_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_ao_basis_ao_value_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_provide_ao_basis_ao_value";
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
@@ -1055,6 +1059,7 @@ qmckl_exit_code_device qmckl_provide_ao_basis_ao_value_device(qmckl_context_devi
 // ---------------------------------------------------------------- results
 qmckl_exit_code_device qmckl_get_ao_basis_shell_vgl_device(qmckl_context_device context, double* const shell_vgl,
                                                            const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_ao_basis_shell_vgl_device");
   Ctx* ctx = checked(context);
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, "qmckl_get_ao_basis_shell_vgl_device", nullptr);
   qmckl_exit_code_device rc = qmckl_provide_ao_basis_shell_vgl_device(context);
@@ -1070,6 +1075,7 @@ qmckl_exit_code_device qmckl_get_ao_basis_shell_vgl_device(qmckl_context_device 
 
 qmckl_exit_code_device qmckl_get_ao_basis_ao_vgl_device(qmckl_context_device context, double* const ao_vgl,
                                                         const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_ao_basis_ao_vgl_device");
   Ctx* ctx = checked(context);
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, "qmckl_get_ao_basis_ao_vgl_device", nullptr);
   qmckl_exit_code_device rc = qmckl_provide_ao_basis_ao_vgl_device(context);
@@ -1088,6 +1094,7 @@ qmckl_exit_code_device qmckl_get_ao_basis_ao_vgl_device(qmckl_context_device con
 // here the result goes straight to the user's buffer and the cache date is untouched.
 qmckl_exit_code_device qmckl_get_ao_basis_ao_vgl_inplace_device(qmckl_context_device context, double* const ao_vgl,
                                                                 const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_ao_basis_ao_vgl_inplace_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_get_ao_basis_ao_vgl_inplace_device";
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
@@ -1106,6 +1113,7 @@ qmckl_exit_code_device qmckl_get_ao_basis_ao_vgl_inplace_device(qmckl_context_de
 
 qmckl_exit_code_device qmckl_get_ao_basis_ao_value_device(qmckl_context_device context, double* const ao_value,
                                                           const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_ao_basis_ao_value_device");
   Ctx* ctx = checked(context);
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, "qmckl_get_ao_basis_ao_value_device", nullptr);
   qmckl_exit_code_device rc = qmckl_provide_ao_basis_ao_value_device(context);
@@ -1121,6 +1129,7 @@ qmckl_exit_code_device qmckl_get_ao_basis_ao_value_device(qmckl_context_device c
 
 qmckl_exit_code_device qmckl_get_ao_basis_ao_value_inplace_device(qmckl_context_device context,
                                                                   double* const ao_value, const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_ao_basis_ao_value_inplace_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_get_ao_basis_ao_value_inplace_device";
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);

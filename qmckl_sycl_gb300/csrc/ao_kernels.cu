@@ -162,12 +162,14 @@ struct Writer {
   int base;                  // AO index of stage slot 0
   int fill;                  // staged AOs
   int cap;                   // capacity of the current window
+  int64_t extent;            // elements of out (bounds-checked build)
 
   __device__ __forceinline__ void init(const FusedArgs& a, Stage<NC>* stage, int64_t p0, int ln, int nv, int64_t p,
                                        int ao_begin) {
     st = stage;
     out = a.out;
     row_len = a.row_len;
+    extent = a.point_num * NC * a.row_len;
     st->pidx[ln] = p;
     nvalid = nv;
     lane = ln;
@@ -186,7 +188,8 @@ struct Writer {
       if (j >= fill) continue;
       const int64_t pt = st->pidx[q];
       const double val = st->v[c][j][q];
-      out[pt * (NC * row_len) + c * row_len + base + j] = val;
+      const int64_t at = pt * (NC * row_len) + c * row_len + base + j;
+      if (QG_STORE_OK(kSiteAoOut, at, extent)) out[at] = val;
     }
     __syncwarp();
     base += fill;
@@ -223,10 +226,12 @@ struct Writer<Out::Planes> {
   int base;                  // AO index of the next emit
   int fill;
   bool valid;                // the lane holds a point
+  int64_t slot;              // p0 + lane: offset of o in the planes (bounds-checked build)
 
   __device__ __forceinline__ void init(const FusedArgs& a, Stage<5>*, int64_t p0, int ln, int nv, int64_t,
                                        int ao_begin) {
     o = static_cast<__nv_bfloat16*>(a.planes) + p0 + ln;
+    slot = p0 + ln;
     pp = (int32_t)a.plane_pp;
     row_len = 5 * a.plane_pp;
     plane_stride = a.row_len * 5 * a.plane_pp;
@@ -238,8 +243,15 @@ struct Writer<Out::Planes> {
     base += fill;
     fill = 0;
   }
+  // Bounds-checked build: the first and last element this emit writes (plane 0 component 0,
+  // plane 2 component 4) lie inside the three planes.
+  __device__ __forceinline__ bool row_ok() const {
+    const int64_t first = slot + (int64_t)(base + fill) * row_len;
+    return QG_STORE_OK(kSiteAoPlanes, first, 3 * plane_stride) &&
+           QG_STORE_OK(kSiteAoPlanes, first + 2 * plane_stride + 4 * pp, 3 * plane_stride);
+  }
   __device__ __forceinline__ void emit(const double (&v)[NC]) {
-    if (valid) {
+    if (valid && row_ok()) {
       // the reference's MO kernel drops an AO whose value is exactly zero from every
       // component of the point (src/qmckl_mo_sycl.cpp:40); tested on the bit pattern (+-0),
       // which keeps the FP64 pipe free
@@ -256,11 +268,12 @@ struct Writer<Out::Planes> {
     }
     fill += 1;
   }
-  // value and gradient already in FP32, Laplacian in FP64; drop: the AO's FP64 value is zero
-  __device__ __forceinline__ void emit_mixed(float v0, float gx, float gy, float gz, double lap, bool drop) {
-    if (valid) {
+  // value, gradient and (assembled in FP64) Laplacian rounded to FP32; drop: the AO's FP64 value
+  // is zero
+  __device__ __forceinline__ void emit_mixed(float v0, float gx, float gy, float gz, float lapf, bool drop) {
+    if (valid && row_ok()) {
       __nv_bfloat16* r = o + (int64_t)(base + fill) * row_len;
-      const float vals[5] = {v0, drop ? 0.f : gx, drop ? 0.f : gy, drop ? 0.f : gz, drop ? 0.f : f64_to_f32(lap)};
+      const float vals[5] = {v0, drop ? 0.f : gx, drop ? 0.f : gy, drop ? 0.f : gz, drop ? 0.f : lapf};
 #pragma unroll
       for (int c = 0; c < NC; ++c) {
         __nv_bfloat16 h, m, l;
@@ -284,6 +297,7 @@ struct ShellVals {
   double t1, t2, t3;  // radial gradient = g * (x, y, z)
   double Rt;   // t4 + 2 l g, the radial part of the Laplacian after Euler's identity
   float Rf, t1f, t2f, t3f;  // FP32 copies for the split-BF16 form's value and gradient
+  bool nan;    // NaN radial sums (NaN coordinate): every output of the shell is NaN
 };
 
 // Powers 0..3 of the displacement from the nucleus, FP64 and (split-BF16 form) FP32.
@@ -367,9 +381,14 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
     }
     // the reference's MO kernel skips an AO whose FP64 value P R f is exactly zero
     // (src/qmckl_mo_sycl.cpp:40): decided on the bits of the factors
-    const bool drop = zero || (bits_of(P) << 1) == 0 || (bits_of(s.R) << 1) == 0 || (bits_of(f) << 1) == 0;
+    bool drop = zero || (bits_of(P) << 1) == 0 || (bits_of(s.R) << 1) == 0 || (bits_of(f) << 1) == 0;
     if (zero) v0 = 0.f;
-    w.emit_mixed(v0, gx, gy, gz, lap, drop);
+    float lapf = f64_to_f32(lap);
+    if (s.nan) {  // the FP64 value is NaN (never skipped); the FP32 conversions would give infinities
+      v0 = gx = gy = gz = lapf = __int_as_float(0x7FC00000);
+      drop = false;
+    }
+    w.emit_mixed(v0, gx, gy, gz, lapf, drop);
     return;
   }
   const double yz = Y[b] * Z[c];
@@ -508,7 +527,12 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     const double x = ex - N.x, y = ey - N.y, z = ez - N.z;
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
     const uint64_t r2b = bits_of(r2);
-    const bool scr = r2b > N.screen_bits;
+    // A NaN coordinate makes r2 NaN. The reference's screening tests (`r2 > cutoff * range`,
+    // `expo * r2 > cutoff`) are false for NaN, so it screens nothing and every primitive gives
+    // exp(NaN) = NaN (src/qmckl_ao_sycl.cpp:53,72-75): such a lane is never screened here, and
+    // the radial sums of its shells with primitives become NaN below.
+    const bool nanr = (r2b << 1) > 0xFFE0000000000000ull;
+    const bool scr = r2b > N.screen_bits && !nanr;
     if (__all_sync(kFull, scr)) {
       w.emit_zeros(N.ao_end - N.ao_begin);
       continue;
@@ -604,6 +628,8 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
         }
       }
       ShellVals sv;
+      sv.nan = nanr && S.prim_end > S.prim_begin;
+      if (sv.nan) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
       sv.R = t0;
       if constexpr (O == Out::Planes) {
         // FP32 value/gradient inputs; the radial part of the Laplacian stays FP64:
@@ -749,7 +775,10 @@ __global__ void shell_vgl_kernel(const NucleusEntry* __restrict__ nuclei, const 
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
   const int64_t os = shell_orig[si];
   double* o = out + ip * 5 * shell_num + os;
-  if (bits_of(r2) > N.screen_bits) {
+  if (!QG_STORE_OK(kSiteShellVgl, ip * 5 * shell_num + os + 4 * shell_num, point_num * 5 * shell_num)) return;
+  // NaN r2 screens nothing, as the reference's `>` tests (every primitive then gives NaN)
+  const bool nanr = (bits_of(r2) << 1) > 0xFFE0000000000000ull;
+  if (bits_of(r2) > N.screen_bits && !nanr) {
     o[0] = o[shell_num] = o[2 * shell_num] = o[3 * shell_num] = o[4 * shell_num] = 0.0;
     return;
   }
@@ -757,7 +786,7 @@ __global__ void shell_vgl_kernel(const NucleusEntry* __restrict__ nuclei, const 
   double t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0;
   for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
     const PrimEntry Pr = prims[pi];
-    if (bits_of(r2) >= Pr.thr_bits) continue;
+    if (bits_of(r2) >= Pr.thr_bits && !nanr) continue;
     const double ar2 = __dmul_rn(Pr.expo, r2);
     const double v = __dmul_rn(Pr.coef, exp(-ar2));
     const double two_a = __dmul_rn(Pr.m2a, v);
@@ -842,7 +871,7 @@ __global__ void cell_scatter_kernel(const int32_t* __restrict__ keys, int64_t P,
   const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= P) return;
   const int pos = atomicAdd(&offsets[keys[p]], 1);
-  perm[pos] = (int32_t)p;
+  if (QG_STORE_OK(kSitePointPerm, pos, P)) perm[pos] = (int32_t)p;
 }
 
 // Picks the first nucleus-chunk level with at least `target` warp tasks.
@@ -970,7 +999,7 @@ __global__ void batch_scatter_kernel(const OrderDesc* __restrict__ desc, const i
   const OrderDesc& d = desc[m];
   const int64_t p = gp - point_begin[m];
   const int pos = atomicAdd(&offsets[(int64_t)m * kOrderCells + d.keys[p]], 1);
-  d.perm[pos] = (int32_t)p;
+  if (QG_STORE_OK(kSitePointPerm, pos, d.point_num)) d.perm[pos] = (int32_t)p;
 }
 
 }  // namespace

@@ -744,6 +744,7 @@ static qmckl_exit_code_device batch_provide(Batch* b, bool force_tune) {
 }
 
 qmckl_exit_code_device qmckl_batch_provide_mo_vgl_device(qmckl_batch_device batch) {
+  QG_NVTX_RANGE("qmckl_batch_provide_mo_vgl_device");
   Batch* b = batch_of(batch);
   if (!b) return QMCKL_INVALID_CONTEXT_DEVICE;
   for (qmckl_context_device h : b->handles)

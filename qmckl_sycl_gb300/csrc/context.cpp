@@ -161,6 +161,44 @@ void* staging(Ctx* ctx, size_t bytes) {
   return ctx->staging;
 }
 
+// The bounds-check records of the translation units (bounds-checked build only).
+static std::vector<void* (*)()>& bounds_records() {
+  static std::vector<void* (*)()> v;
+  return v;
+}
+
+void register_bounds_record(void* (*address)()) { bounds_records().push_back(address); }
+
+int32_t bounds_check_status(bool reset, int64_t* site, int64_t* index, int64_t* extent) {
+#ifndef QMCKL_BOUNDS_CHECK
+  (void)reset;
+  (void)site;
+  (void)index;
+  (void)extent;
+  return -1;
+#else
+  struct Rec {
+    int hit, site;
+    long long index, extent;
+  };
+  int32_t found = 0;
+  for (auto address : bounds_records()) {
+    void* p = address();
+    if (!p) return -2;
+    Rec r{};
+    if (cudaMemcpy(&r, p, sizeof r, cudaMemcpyDeviceToHost) != cudaSuccess) return -2;
+    if (r.hit && !found) {
+      found = 1;
+      if (site) *site = r.site;
+      if (index) *index = r.index;
+      if (extent) *extent = r.extent;
+    }
+    if (reset && cudaMemset(p, 0, sizeof r) != cudaSuccess) return -2;
+  }
+  return found;
+#endif
+}
+
 }  // namespace qg
 
 extern "C" {
@@ -624,6 +662,41 @@ qmckl_exit_code_device qmckl_set_allocation_failure_device(qmckl_context_device 
   return QMCKL_SUCCESS_DEVICE;
 }
 
-const char* qmckl_gb300_build_info(void) { return "qmckl-gb300 sm_103a fp64+split-bf16"; }
+int32_t qmckl_bounds_check_status_device(int32_t reset, int64_t* site, int64_t* index, int64_t* extent) {
+  return qg::bounds_check_status(reset != 0, site, index, extent);
+}
+
+int32_t qmckl_bounds_check_selftest_device(int64_t index, int64_t extent) {
+#ifndef QMCKL_BOUNDS_CHECK
+  (void)index;
+  (void)extent;
+  return -1;
+#else
+  return qg::bounds_selftest(index, extent) == cudaSuccess ? 0 : -2;
+#endif
+}
+
+qmckl_exit_code_device qmckl_set_split_wait_test_device(qmckl_context_device context, int64_t wait_cycles,
+                                                        int32_t withhold_loads) {
+  if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
+  if (wait_cycles < 0)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, "qmckl_set_split_wait_test_device",
+                                 "wait_cycles must be >= 0");
+  if (withhold_loads != 0 && withhold_loads != 1)
+    return qmckl_failwith_device(context, QMCKL_INVALID_ARG_3_DEVICE, "qmckl_set_split_wait_test_device",
+                                 "withhold_loads must be 0 or 1");
+  Ctx* ctx = ctx_of(context);
+  ctx->split_wait_cycles = wait_cycles;
+  ctx->split_withhold_loads = withhold_loads;
+  return QMCKL_SUCCESS_DEVICE;
+}
+
+const char* qmckl_gb300_build_info(void) {
+#ifdef QMCKL_BOUNDS_CHECK
+  return "qmckl-gb300 sm_103a fp64+split-bf16 bounds-check";
+#else
+  return "qmckl-gb300 sm_103a fp64+split-bf16";
+#endif
+}
 
 }  // extern "C"

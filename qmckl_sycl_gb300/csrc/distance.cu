@@ -29,7 +29,8 @@ __global__ void distance_kernel(const double* __restrict__ A, bool ta, int64_t l
   const double y = __dsub_rn(coord_of(A, ta, lda, w * a_step + i, 1), coord_of(B, tb, ldb, w * b_step + j, 1));
   const double z = __dsub_rn(coord_of(A, ta, lda, w * a_step + i, 2), coord_of(B, tb, ldb, w * b_step + j, 2));
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
-  C[w * c_step + i + j * ldc] = __dsqrt_rn(r2);
+  if (QG_STORE_OK(kSiteDistance, w * c_step + i + j * ldc, (total / (m * n) - 1) * c_step + (n - 1) * ldc + m))
+    C[w * c_step + i + j * ldc] = __dsqrt_rn(r2);
 }
 
 // The reference's argument checks (src/qmckl_electron.cpp:380-488), with lda checked against transa
@@ -70,6 +71,7 @@ extern "C" {
 qmckl_exit_code_device qmckl_distance_device(const qmckl_context_device context, const char transa, const char transb,
                                              const int64_t m, const int64_t n, const double* A, const int64_t lda,
                                              const double* B, const int64_t ldb, double* const C, const int64_t ldc) {
+  QG_NVTX_RANGE("qmckl_distance_device");
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   bool ta = false, tb = false;
   qmckl_exit_code_device rc = check_distance_args(transa, transb, m, n, lda, ldb, ldc, &ta, &tb);
@@ -87,6 +89,7 @@ qmckl_exit_code_device qmckl_distance_device(const qmckl_context_device context,
 qmckl_exit_code_device qmckl_compute_en_distance_device(const qmckl_context_device context, const int64_t point_num,
                                                         const int64_t nucl_num, const double* elec_coord,
                                                         const double* nucl_coord, double* const en_distance) {
+  QG_NVTX_RANGE("qmckl_compute_en_distance_device");
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (point_num <= 0) return QMCKL_INVALID_ARG_2_DEVICE;
   if (nucl_num <= 0) return QMCKL_INVALID_ARG_3_DEVICE;
@@ -99,6 +102,7 @@ qmckl_exit_code_device qmckl_compute_en_distance_device(const qmckl_context_devi
 qmckl_exit_code_device qmckl_compute_ee_distance_device(const qmckl_context_device context, const int64_t elec_num,
                                                         const int64_t walk_num, const double* coord,
                                                         double* const ee_distance) {
+  QG_NVTX_RANGE("qmckl_compute_ee_distance_device");
   const char* fn = "qmckl_compute_ee_distance_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (elec_num <= 0) return QMCKL_INVALID_ARG_2_DEVICE;
@@ -118,6 +122,7 @@ qmckl_exit_code_device qmckl_compute_ee_distance_device(const qmckl_context_devi
 }
 
 qmckl_exit_code_device qmckl_provide_en_distance_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_en_distance_device");
   const char* fn = "qmckl_provide_en_distance_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   Ctx* ctx = ctx_of(context);
@@ -137,6 +142,7 @@ qmckl_exit_code_device qmckl_provide_en_distance_device(qmckl_context_device con
 }
 
 qmckl_exit_code_device qmckl_provide_ee_distance_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_ee_distance_device");
   const char* fn = "qmckl_provide_ee_distance_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   Ctx* ctx = ctx_of(context);
@@ -158,6 +164,7 @@ qmckl_exit_code_device qmckl_provide_ee_distance_device(qmckl_context_device con
 
 qmckl_exit_code_device qmckl_get_electron_en_distance_device(qmckl_context_device context, double* distance,
                                                              int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_electron_en_distance_device");
   const char* fn = "qmckl_get_electron_en_distance_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (!distance) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, fn, "NULL pointer");
@@ -171,6 +178,7 @@ qmckl_exit_code_device qmckl_get_electron_en_distance_device(qmckl_context_devic
 
 qmckl_exit_code_device qmckl_get_electron_ee_distance_device(qmckl_context_device context, double* distance,
                                                              int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_electron_ee_distance_device");
   const char* fn = "qmckl_get_electron_ee_distance_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (!distance) return qmckl_failwith_device(context, QMCKL_INVALID_ARG_2_DEVICE, fn, "NULL pointer");

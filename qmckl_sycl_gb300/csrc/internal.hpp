@@ -4,6 +4,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <mutex>
@@ -12,8 +13,19 @@
 #include <vector>
 
 #include "../../include/qmckl_gpu.h"
+#include "bounds.cuh"
 
 namespace qg {
+
+// NVTX range around a C-ABI entry point (header-only NVTX 3: a no-op unless a profiler such as
+// ncu or Nsight Systems is attached), so that a timeline shows each call with its kernels.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define QG_NVTX_RANGE(name) ::qg::NvtxRange qg_nvtx_range_(name)
 
 constexpr uint64_t kValidTag = 0xBEEFFACEull;    // include/qmckl_types.hpp:12 of the reference
 constexpr uint64_t kInvalidTag = 0xDEADBEEFull;  // include/qmckl_types.hpp:13
@@ -276,6 +288,10 @@ struct qmckl_context_struct_device {
   size_t vjp_cap = 0;
   // task counter of the persistent AO kernels (zeroed before each launch)
   unsigned long long* task_counter = nullptr;
+  // failure-handling test hook of the split-BF16 contraction (qmckl_set_split_wait_test_device):
+  // wait limit in clock cycles (0: the default, ~1 s) and a producer that issues no loads
+  int64_t split_wait_cycles = 0;
+  int32_t split_withhold_loads = 0;
 
   // profiling
   bool profiling = false;
@@ -315,6 +331,10 @@ bool ensure_device(Ctx* ctx);
 bool gpu_accessible(const void* p);
 // The context's grow-only staging buffer, at least `bytes` long (nullptr on failure).
 void* staging(Ctx* ctx, size_t bytes);
+// First recorded out-of-range store of the bounds-checked build over all translation units
+// (1 found, 0 none, -1 not a bounds-checked build, -2 a CUDA error); reset clears the records.
+int32_t bounds_check_status(bool reset, int64_t* site, int64_t* index, int64_t* extent);
+cudaError_t bounds_selftest(int64_t index, int64_t extent);
 
 // Synchronous unless ctx->async.
 qmckl_exit_code_device finish(Ctx* ctx, qmckl_context_device c, const char* fn);

@@ -25,6 +25,7 @@ Ctx* checked(qmckl_context_device c) {
 extern "C" {
 
 qmckl_exit_code_device qmckl_finalize_mo_basis_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_finalize_mo_basis_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_finalize_mo_basis_device";
   if (!ctx) return qmckl_failwith_device(context, QMCKL_INVALID_CONTEXT_DEVICE, fn, nullptr);
@@ -169,6 +170,7 @@ static qmckl_exit_code_device compute_mo_value(Ctx* ctx, qmckl_context_device co
 }
 
 qmckl_exit_code_device qmckl_provide_mo_basis_mo_vgl_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_mo_basis_mo_vgl_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
@@ -185,6 +187,7 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_vgl_device(qmckl_context_device
 }
 
 qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_device context) {
+  QG_NVTX_RANGE("qmckl_provide_mo_basis_mo_value_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_provide_mo_basis_mo_value_device";
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
@@ -212,6 +215,7 @@ static bool host_memory(const void* p) {
 
 qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device context, double* const mo_vgl,
                                                         const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_mo_basis_mo_vgl_device");
   Ctx* ctx = checked(context);
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
   MoBasisData& mo = ctx->mo_basis;
@@ -240,6 +244,7 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
 
 qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_inplace_device(qmckl_context_device context, double* const mo_vgl,
                                                                 const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_mo_basis_mo_vgl_inplace_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_get_mo_basis_mo_vgl_device";
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
@@ -258,6 +263,7 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_inplace_device(qmckl_context_de
 
 qmckl_exit_code_device qmckl_get_mo_basis_mo_value_device(qmckl_context_device context, double* const mo_value,
                                                           const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_mo_basis_mo_value_device");
   Ctx* ctx = checked(context);
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;
   qmckl_exit_code_device rc = qmckl_provide_mo_basis_mo_value_device(context);
@@ -272,6 +278,7 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_value_device(qmckl_context_device c
 
 qmckl_exit_code_device qmckl_get_mo_basis_mo_value_inplace_device(qmckl_context_device context,
                                                                   double* const mo_value, const int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_get_mo_basis_mo_value_inplace_device");
   Ctx* ctx = checked(context);
   const char* fn = "qmckl_get_mo_basis_mo_value_device";
   if (!ctx) return QMCKL_INVALID_CONTEXT_DEVICE;

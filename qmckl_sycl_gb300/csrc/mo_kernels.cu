@@ -92,8 +92,9 @@ __device__ __forceinline__ void dgemm_warp_tile(const double* __restrict__ A, in
       for (int h = 0; h < 2; ++h) {
         const int64_t row = r0 + 16 * i + g + 8 * h;
         if (row < R) {
-          if (col < N) C[row * N + col] = acc[i][j][2 * h];
-          if (col + 1 < N) C[row * N + col + 1] = acc[i][j][2 * h + 1];
+          if (col < N && QG_STORE_OK(kSiteDgemmOut, row * N + col, R * N)) C[row * N + col] = acc[i][j][2 * h];
+          if (col + 1 < N && QG_STORE_OK(kSiteDgemmOut, row * N + col + 1, R * N))
+            C[row * N + col + 1] = acc[i][j][2 * h + 1];
         }
       }
     }
@@ -126,7 +127,7 @@ __global__ void sum_parts_kernel(const double* __restrict__ parts, int nparts, i
   if (i >= n) return;
   double s = 0.0;
   for (int z = 0; z < nparts; ++z) s += parts[(int64_t)z * n + i];
-  out[i] = s;
+  if (QG_STORE_OK(kSiteSumParts, i, n)) out[i] = s;
 }
 
 // Several contractions, persistent: a CTA of WR x WC warps owns (32 WR) x (32 WC) tiles of C,

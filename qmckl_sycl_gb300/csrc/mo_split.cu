@@ -68,6 +68,14 @@ constexpr int kTPitch = 9;                   // transposition buffer: 32 rows x 
 constexpr uint32_t kTBuf = 32 * kTPitch * 4;  // bytes per fold warp
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
 
+// Launch controls of the contraction kernel: the limit of every mbarrier wait (clock cycles),
+// and, for the failure-handling test only, a producer that issues no loads, so that the
+// consumers' first wait is one that nothing completes and runs out (no load is in flight then).
+struct SplitCtl {
+  long long wait_cycles = kWaitCycles;
+  int32_t withhold_loads = 0;
+};
+
 // ------------------------------------------------------------------ split helpers
 // Double -> float, round to nearest even, by integer operations on the bit pattern (no FP64
 // instruction). Values below the float normal range flush to a signed zero; AO and MO
@@ -150,6 +158,7 @@ __global__ void split_planes_kernel(const double* __restrict__ src, int64_t rows
     }
     __nv_bfloat16 h, m, l;
     split3(a, h, m, l);
+    if (!QG_STORE_OK(kSiteSplitPlanes, 2 * plane + i, 3 * plane)) continue;
     planes[i] = h;
     planes[plane + i] = m;
     planes[2 * plane + i] = l;
@@ -174,11 +183,11 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: true when the phase completed, false after ~1 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait: true when the phase completed, false after `limit` cycles (~1 s by default).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity)) {
-    if (clock64() - t0 > kWaitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -320,10 +329,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 }
 
 // Bounded wait that also gives up once another role has aborted.
-__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                              long long limit) {
   const long long t0 = clock64();
   while (!mbar_try(bar, parity)) {
-    if (*abort_flag || clock64() - t0 > kWaitCycles) return false;
+    if (*abort_flag || clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -367,6 +377,7 @@ struct FoldCtx {
   uint64_t *accf, *acce, *tmem_free;
   volatile int* abort_flag;
   int* error;
+  long long wait_cycles;
   int lane, quarter, half;
 };
 
@@ -442,7 +453,7 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
   for (int kb = 0; kb < groups; ++kb, ++it) {
     const uint32_t b = it % kBufs, use = it / kBufs;
     // warp-uniform decision: the tcgen05.ld below are .sync.aligned
-    if (!__all_sync(0xffffffffu, wait_or_abort(&f.accf[b], use & 1u, f.abort_flag))) {
+    if (!__all_sync(0xffffffffu, wait_or_abort(&f.accf[b], use & 1u, f.abort_flag, f.wait_cycles))) {
       if (f.lane == 0) set_abort(f.abort_flag, f.error, 4);
       return false;
     }
@@ -503,6 +514,8 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
 
   const int64_t c_first = (int64_t)tr.n0 + hc;  // first output column of this warp
   const int ncol = (int)(job.cols - c_first < nh ? job.cols - c_first : nh);  // valid columns (may be <= 0)
+  // elements of the output (bounds-checked build): 5 npts rows (M-major A) or rows
+  const int64_t out_extent = (job.a_mn ? 5 * job.npts : job.rows) * job.ldo;
   if ((reinterpret_cast<uintptr_t>(job.out) & 31) == 0 && (job.ldo & 3) == 0 && (c_first & 3) == 0) {
     // 32-byte aligned row segments: each lane writes its own row, four columns per 32-byte
     // store, straight from registers (shared memory is busy with the MMAs' operand reads and
@@ -512,6 +525,7 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
 #pragma unroll
       for (int c0 = 0; c0 < kHalfN; c0 += 4) {
         if (c0 + 4 <= ncol) {
+          if (!QG_STORE_OK(kSiteSplitOut, orow * job.ldo + c_first + c0 + 3, out_extent)) continue;
           const float v0 = lo_f(h2[c0 >> 1]), v1 = hi_f(h2[c0 >> 1]), v2 = lo_f(h2[(c0 >> 1) + 1]),
                       v3 = hi_f(h2[(c0 >> 1) + 1]);
           if (f32_special(v0) || f32_special(v1) || f32_special(v2) || f32_special(v3))
@@ -522,7 +536,8 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
         } else if (c0 < ncol) {
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            if (c0 + j < ncol) p[c0 + j] = f32_to_f64_int(j & 1 ? hi_f(h2[(c0 + j) >> 1]) : lo_f(h2[(c0 + j) >> 1]));
+            if (c0 + j < ncol && QG_STORE_OK(kSiteSplitOut, orow * job.ldo + c_first + c0 + j, out_extent))
+              p[c0 + j] = f32_to_f64_int(j & 1 ? hi_f(h2[(c0 + j) >> 1]) : lo_f(h2[(c0 + j) >> 1]));
         }
       }
     }
@@ -548,7 +563,9 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const float v = tb[(4 * i + rr) * kTPitch + cc];
-        if (orows[i] >= 0 && col_ok) out[orows[i] * ldo + c0] = f32_to_f64_int(v);
+        if (orows[i] >= 0 && col_ok &&
+            QG_STORE_OK(kSiteSplitOut, orows[i] * ldo + c_first + cc + c0, out_extent))
+          out[orows[i] * ldo + c0] = f32_to_f64_int(v);
       }
       __syncwarp();
     }
@@ -564,7 +581,7 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
 // warps have read the previous tile's corrections out of tensor memory (they then write that
 // tile's output while the next tile computes).
 __global__ void __launch_bounds__(kThreads, 1)
-    split_gemm_kernel(const SplitJob* __restrict__ jobs, int njobs, int total_tiles, int* error) {
+    split_gemm_kernel(const SplitJob* __restrict__ jobs, int njobs, int total_tiles, int* error, const SplitCtl ctl) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   float* tbuf = (float*)(base + kStages * kMaxStage);
@@ -617,11 +634,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t stage_bytes = 3 * kPlaneA + 3 * plane_b;
         for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
           const uint32_t s2 = it % kStages, ph = (it / kStages) & 1u;
-          if (!wait_or_abort(&empty[s2], ph ^ 1u, abort_flag)) {
+          if (!wait_or_abort(&empty[s2], ph ^ 1u, abort_flag, ctl.wait_cycles)) {
             set_abort(abort_flag, error, 1);
             ok = false;
             break;
           }
+          if (ctl.withhold_loads) continue;  // failure-handling test: nothing completes `full`
           unsigned char* st = base + s2 * kMaxStage;
           mbar_expect_tx(&full[s2], stage_bytes);
           if (job.a_mn) {
@@ -639,7 +657,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       // the loads still in flight must land before the shared memory is released
       const uint32_t first = it > (uint32_t)kStages ? it - kStages : 0;
-      for (uint32_t q = first; q < it; ++q) mbar_wait(&full[q % kStages], (q / kStages) & 1u);
+      if (!ctl.withhold_loads)
+        for (uint32_t q = first; q < it; ++q) mbar_wait(&full[q % kStages], (q / kStages) & 1u, ctl.wait_cycles);
     }
   } else if (warp == 1) {
     reg_dec<kRegsIssue>();
@@ -658,7 +677,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const bool amn = job.a_mn != 0;
         const uint64_t ka = amn ? 128u : 2u, pa = kPlaneA >> 4, pb = plane_b >> 4;
         // the correction accumulator is read out before reuse
-        if (tl > 0 && !wait_or_abort(tmem_free, (tl - 1) & 1u, abort_flag)) {
+        if (tl > 0 && !wait_or_abort(tmem_free, (tl - 1) & 1u, abort_flag, ctl.wait_cycles)) {
           set_abort(abort_flag, error, 6);
           break;
         }
@@ -666,12 +685,12 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int kb = 0; kb < job.kblocks; ++kb, ++it) {
           const uint32_t s2 = it % kStages, ph = (it / kStages) & 1u, b = gi % kBufs, use = gi / kBufs;
           const bool first = kb % kFold == 0, last = kb % kFold == kFold - 1 || kb == job.kblocks - 1;
-          if (first && use > 0 && !wait_or_abort(&acce[b], (use - 1) & 1u, abort_flag)) {
+          if (first && use > 0 && !wait_or_abort(&acce[b], (use - 1) & 1u, abort_flag, ctl.wait_cycles)) {
             set_abort(abort_flag, error, 2);
             ok = false;
             break;
           }
-          if (!wait_or_abort(&full[s2], ph, abort_flag)) {
+          if (!wait_or_abort(&full[s2], ph, abort_flag, ctl.wait_cycles)) {
             set_abort(abort_flag, error, 3);
             ok = false;
             break;
@@ -698,7 +717,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
       umma_commit(mma_done);  // every MMA issued has completed
-      if (!mbar_wait(mma_done, 0)) set_abort(abort_flag, error, 5);
+      if (!mbar_wait(mma_done, 0, ctl.wait_cycles)) set_abort(abort_flag, error, 5);
     }
   } else if (warp < 4) {
     reg_dec<kRegsIssue>();  // warps 2 and 3: no role (they complete warpgroup 0)
@@ -708,7 +727,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // and column half (w - 4) / 4 of each tile
     const int quarter = warp & 3, half = (warp - 4) >> 2;
     FoldCtx f{tmem + ((uint32_t)(quarter * 32) << 16), tbuf + (size_t)(warp - 4) * 32 * kTPitch, accf, acce,
-              tmem_free, abort_flag, error, lane, quarter, half};
+              tmem_free, abort_flag, error, ctl.wait_cycles, lane, quarter, half};
     uint32_t it = 0;
     bool ok = true;
     for (int tile = blockIdx.x; ok && tile < total_tiles; tile += gridDim.x) {
@@ -731,19 +750,18 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// Resolved once per process; the initialisation of a function-local static is thread-safe, so
+// first calls from several host threads (one per device, say) all see the resolved pointer.
 EncodeTiledFn encode_tiled_fn() {
-  static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-    else
-      cudaGetLastError();
-  }
+      return reinterpret_cast<EncodeTiledFn>(p);
+    cudaGetLastError();
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -833,8 +851,10 @@ int make_job_mn(SplitJob& job, const __nv_bfloat16* ap, int64_t pp, int64_t npts
 
 size_t split_smem_bytes() { return 1024 + kStages * (size_t)kMaxStage + 8 * (size_t)kTBuf + 256; }
 
-// One persistent launch over every tile of the njobs jobs at d_jobs (device memory).
-cudaError_t launch_split_jobs(cudaStream_t stream, const SplitJob* d_jobs, int njobs, int total_tiles, int* err) {
+// One persistent launch over every tile of the njobs jobs at d_jobs (device memory). Returns
+// the launch's own status (cudaLaunchKernel), not an earlier error pending in the runtime.
+cudaError_t launch_split_jobs(cudaStream_t stream, const SplitJob* d_jobs, int njobs, int total_tiles, int* err,
+                              const SplitCtl& ctl = SplitCtl{}) {
   if (total_tiles <= 0) return cudaSuccess;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
@@ -842,8 +862,8 @@ cudaError_t launch_split_jobs(cudaStream_t stream, const SplitJob* d_jobs, int n
   const size_t smem = split_smem_bytes();
   cudaFuncSetAttribute(split_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int grid = total_tiles < sms ? total_tiles : sms;
-  split_gemm_kernel<<<grid, kThreads, smem, stream>>>(d_jobs, njobs, total_tiles, err);
-  return cudaGetLastError();
+  void* args[] = {(void*)&d_jobs, (void*)&njobs, (void*)&total_tiles, (void*)&err, (void*)&ctl};
+  return cudaLaunchKernel((const void*)split_gemm_kernel, dim3(grid), dim3(kThreads), args, smem, stream);
 }
 
 cudaError_t launch_split(Ctx* ctx, const double* src, int64_t rows, int64_t k, int64_t ld, int64_t kp, bool mask5,
@@ -855,6 +875,14 @@ cudaError_t launch_split(Ctx* ctx, const double* src, int64_t rows, int64_t k, i
   LaunchScope scope(ctx, mask5 ? "split_ao_planes" : "split_planes");
   split_planes_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(src, rows, k, ld, kp, mask5 ? 1 : 0, planes);
   return cudaGetLastError();
+}
+
+// The context's launch controls (the failure-handling test hook, when set).
+SplitCtl ctl_of(const Ctx* ctx) {
+  SplitCtl c;
+  if (ctx->split_wait_cycles > 0) c.wait_cycles = ctx->split_wait_cycles;
+  c.withhold_loads = ctx->split_withhold_loads;
+  return c;
 }
 
 }  // namespace
@@ -887,7 +915,7 @@ static qmckl_exit_code_device run_job(Ctx* ctx, qmckl_context_device c, const Sp
   }
   {
     LaunchScope scope(ctx, name);
-    launch_split_jobs(ctx->stream, static_cast<const SplitJob*>(mo.split_job), 1, tiles, err);
+    launch_split_jobs(ctx->stream, static_cast<const SplitJob*>(mo.split_job), 1, tiles, err, ctl_of(ctx));
   }
   qmckl_exit_code_device rc = finish(ctx, c, fn);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -1051,7 +1079,7 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
     launch_ao_planes(ctx, ao.tables, coord, P, ao.point_perm, n, kp, ap);
     {
       LaunchScope scope(ctx, "mo_vgl_split_bf16");
-      launch_split_jobs(ctx->stream, d_jobs + k, 1, tiles[k], err);
+      launch_split_jobs(ctx->stream, d_jobs + k, 1, tiles[k], err, ctl_of(ctx));
     }
     cudaEventRecord(done[k], ctx->stream);
     cudaStreamWaitEvent(ctx->copy_stream, done[k], 0);
@@ -1102,6 +1130,10 @@ constexpr size_t kNoAllocBytes =
     sizeof(__nv_bfloat16) * 3 * (size_t)(kNoAllocMaxMo + kNoAllocChunkRows) * (size_t)kNoAllocMaxAo + 2048;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+// Layout of the array: B planes [3][mo_num][kp], A planes [3][chunk rows][kp] (together at most
+// kNoAllocBytes - 2048 bytes), the job descriptor at kNoAllocBytes - 2048, the error word at
+// kNoAllocBytes - 256.
+static_assert(sizeof(SplitJob) <= 2048 - 256, "the job descriptor must end below the error word");
 
 // Host-side device addresses of the array, one per device, resolved on each device's first
 // call (with that device current). A host pointer to the symbol is not a device address.
@@ -1130,19 +1162,13 @@ extern "C" qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(co
   cudaStream_t stream = static_cast<cudaStream_t>(cuda_stream);
 
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
-    cudaGetLastError();
-    return QMCKL_FAILURE_DEVICE;
-  }
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) return QMCKL_FAILURE_DEVICE;
   void* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
     if (!g_noalloc_ptr[dev]) {
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-        cudaGetLastError();
-        return QMCKL_FAILURE_DEVICE;
-      }
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return QMCKL_FAILURE_DEVICE;
       g_noalloc_ptr[dev] = p;
     }
     scratch = g_noalloc_ptr[dev];
@@ -1153,39 +1179,36 @@ extern "C" qmckl_exit_code_device qmckl_mo_contract_split_bf16_noalloc_device(co
   __nv_bfloat16* bplanes = static_cast<__nv_bfloat16*>(scratch);
   __nv_bfloat16* aplanes = bplanes + 3 * M * kp;
   int* err = reinterpret_cast<int*>(static_cast<unsigned char*>(scratch) + kNoAllocBytes - 256);
-  if (cudaMemsetAsync(err, 0, sizeof(int), stream) != cudaSuccess) {
-    cudaGetLastError();
-    return QMCKL_FAILURE_DEVICE;
-  }
+  if (cudaMemsetAsync(err, 0, sizeof(int), stream) != cudaSuccess) return QMCKL_FAILURE_DEVICE;
 
   SplitJob* djob = reinterpret_cast<SplitJob*>(static_cast<unsigned char*>(scratch) + kNoAllocBytes - 2048);
 
+  // Every launch's own status is checked where it is issued (cudaLaunchKernel returns it), so an
+  // error pending from the caller's earlier work is neither reported as this call's nor cleared.
   auto split = [&](const double* src, int64_t n, int64_t ld, bool mask, __nv_bfloat16* dst) {
     int64_t blocks = (n * kp + 255) / 256;
     if (blocks > 152 * 64) blocks = 152 * 64;
-    split_planes_kernel<<<(unsigned)blocks, 256, 0, stream>>>(src, n, ao_num, ld, kp, mask ? 1 : 0, dst);
+    int64_t k = ao_num;
+    int m5 = mask ? 1 : 0;
+    void* args[] = {(void*)&src, (void*)&n, (void*)&k, (void*)&ld, (void*)&kp, (void*)&m5, (void*)&dst};
+    return cudaLaunchKernel((const void*)split_planes_kernel, dim3((unsigned)blocks), dim3(256), args, 0, stream);
   };
-  split(coefficient, M, ao_num, false, bplanes);
+  if (split(coefficient, M, ao_num, false, bplanes) != cudaSuccess) return QMCKL_FAILURE_DEVICE;
 
   for (int64_t r0 = 0; r0 < rows; r0 += kNoAllocChunkRows) {
     const int64_t n = rows - r0 < kNoAllocChunkRows ? rows - r0 : kNoAllocChunkRows;
-    split(ao + r0 * ao_num, n, ao_num, vgl_mask != 0, aplanes);
+    if (split(ao + r0 * ao_num, n, ao_num, vgl_mask != 0, aplanes) != cudaSuccess) return QMCKL_FAILURE_DEVICE;
     SplitJob job;
     const int tiles = make_job(job, aplanes, n, bplanes, M, kp, out + r0 * M, 0);
     if (tiles < 0) return QMCKL_FAILURE_DEVICE;
     // the descriptor lives in the array too; the copy is ordered after the previous chunk's kernel
-    if (cudaMemcpyAsync(djob, &job, sizeof job, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
-      cudaGetLastError();
+    if (cudaMemcpyAsync(djob, &job, sizeof job, cudaMemcpyHostToDevice, stream) != cudaSuccess)
       return QMCKL_FAILURE_DEVICE;
-    }
-    launch_split_jobs(stream, djob, 1, tiles, err);
+    if (launch_split_jobs(stream, djob, 1, tiles, err) != cudaSuccess) return QMCKL_FAILURE_DEVICE;
   }
   int h = 0;
-  if (cudaGetLastError() != cudaSuccess ||
-      cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-      cudaStreamSynchronize(stream) != cudaSuccess) {
-    cudaGetLastError();
+  if (cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
     return QMCKL_FAILURE_DEVICE;
-  }
   return h ? QMCKL_FAILURE_DEVICE : QMCKL_SUCCESS_DEVICE;
 }

@@ -53,6 +53,7 @@ extern "C" {
 // ---------------------------------------------------------------- points
 qmckl_exit_code_device qmckl_set_point_device(qmckl_context_device context, char transp, int64_t num, double* coord,
                                               int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_set_point_device");
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   if (size_max < 3 * num)
     return qmckl_failwith_device(context, QMCKL_INVALID_ARG_4_DEVICE, "qmckl_set_point_device", "Array too small");
@@ -263,6 +264,7 @@ qmckl_exit_code_device qmckl_set_electron_num_device(qmckl_context_device contex
 
 qmckl_exit_code_device qmckl_set_electron_coord_device(qmckl_context_device context, char transp, int64_t walk_num,
                                                        double* coord, int64_t size_max) {
+  QG_NVTX_RANGE("qmckl_set_electron_coord_device");
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   Ctx* ctx = ctx_of(context);
   const int64_t elec_num = ctx->electron.num;

@@ -22,7 +22,8 @@ __global__ void transpose_kernel(const double* __restrict__ in, int64_t rows, in
   __syncthreads();
   for (int i = threadIdx.y; i < 32; i += blockDim.y) {
     const int64_t c = bx + i, r = by + threadIdx.x;
-    if (c < cols && r < rows) out[c * rows + r] = tile[threadIdx.x][i];
+    if (c < cols && r < rows && QG_STORE_OK(kSiteUtil, c * rows + r, rows * cols))
+      out[c * rows + r] = tile[threadIdx.x][i];
   }
 }
 
@@ -38,6 +39,12 @@ __global__ void strided_copy_kernel(const double* __restrict__ in, int64_t in_st
 __global__ void fill_kernel(double* __restrict__ p, int64_t n, double v) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = v;
+}
+
+// Self-test of the bounds-checked build's recording: evaluates the check for element `index` of
+// an array of `extent` elements and stores nothing (there is no array).
+__global__ void bounds_selftest_kernel(long long index, long long extent) {
+  if (QG_STORE_OK(kSiteUtil, index, extent)) return;
 }
 
 unsigned grid_for(int64_t n) {
@@ -69,6 +76,14 @@ cudaError_t launch_fill(Ctx* ctx, double* p, int64_t n, double v) {
   LaunchScope scope(ctx, "fill");
   fill_kernel<<<grid_for(n), 256, 0, ctx->stream>>>(p, n, v);
   return cudaGetLastError();
+}
+
+// Launches the self-test on the current device and waits for it (bounds-checked build; the
+// normal build's check is the constant `true`, so the kernel then does nothing).
+cudaError_t bounds_selftest(int64_t index, int64_t extent) {
+  bounds_selftest_kernel<<<1, 1>>>((long long)index, (long long)extent);
+  cudaError_t e = cudaGetLastError();
+  return e != cudaSuccess ? e : cudaDeviceSynchronize();
 }
 
 // in[num][3] -> out[3][num]

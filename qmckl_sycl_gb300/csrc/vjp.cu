@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(kVjpWarps * 32) vjp_ao_kernel(const VjpArgs a)
   Reader rd{st, a.gbar, a.ao_num, nvalid, lane, 0, 0};
   double de[3] = {0.0, 0.0, 0.0};
   double* apart = wa ? a.alpha_part + group * (int64_t)a.prim_num : nullptr;
+  const int64_t apart_extent = (P + 31) / 32 * (int64_t)a.prim_num;  // bounds-checked build
   const NucleusChunk cj = a.chunks[ch];
 
   for (int n = cj.nucl_begin; n < cj.nucl_end; ++n) {
@@ -293,7 +294,8 @@ __global__ void __launch_bounds__(kVjpWarps * 32) vjp_ao_kernel(const VjpArgs a)
     if (__all_sync(kFull, scr)) {
       if (wa && N.shell_end > N.shell_begin) {
         const int k0 = a.shells[N.shell_begin].prim_begin, k1 = a.shells[N.shell_end - 1].prim_end;
-        for (int k = k0 + lane; k < k1; k += 32) apart[k] = 0.0;
+        for (int k = k0 + lane; k < k1; k += 32)
+          if (QG_STORE_OK(kSiteVjp, group * (int64_t)a.prim_num + k, apart_extent)) apart[k] = 0.0;
       }
       continue;
     }
@@ -357,13 +359,14 @@ __global__ void __launch_bounds__(kVjpWarps * 32) vjp_ao_kernel(const VjpArgs a)
             val = act ? t : 0.0;
           }
           val = warp_sum(val);
-          if (lane == 0) apart[pi] = val;
+          if (lane == 0 && QG_STORE_OK(kSiteVjp, group * (int64_t)a.prim_num + pi, apart_extent)) apart[pi] = val;
         }
       }
     }
   }
   if (wc && lane < nvalid) {
     double* o = a.coord_part + ((int64_t)ch * P + p) * 3;
+    if (!QG_STORE_OK(kSiteVjp, ((int64_t)ch * P + p) * 3 + 2, (int64_t)a.chunk_num * P * 3)) return;
     o[0] = de[0];
     o[1] = de[1];
     o[2] = de[2];
@@ -372,11 +375,13 @@ __global__ void __launch_bounds__(kVjpWarps * 32) vjp_ao_kernel(const VjpArgs a)
 
 // d_exponent[prim_orig[k]] (+)= sum over point groups (in order) of part[g][k].
 __global__ void reduce_alpha_kernel(const double* __restrict__ part, int64_t groups, int K,
-                                    const int32_t* __restrict__ prim_orig, int unique, double* __restrict__ out) {
+                                    const int32_t* __restrict__ prim_orig, int unique, double* __restrict__ out,
+                                    int64_t out_num) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
   double s = 0.0;
   for (int64_t g = 0; g < groups; ++g) s += part[g * K + k];
+  if (!QG_STORE_OK(kSiteVjp, prim_orig[k], out_num)) return;
   if (unique) out[prim_orig[k]] = s;
   else atomicAdd(out + prim_orig[k], s);
 }
@@ -387,7 +392,7 @@ __global__ void reduce_coord_kernel(const double* __restrict__ part, int chunks,
   if (i >= n) return;
   double s = 0.0;
   for (int c = 0; c < chunks; ++c) s += part[(int64_t)c * n + i];
-  out[i] = s;
+  if (QG_STORE_OK(kSiteVjp, i, n)) out[i] = s;
 }
 
 // aoM = ao_vgl with the zero-value skip applied: rows 5p+1..5p+4 zero where row 5p is zero.
@@ -397,7 +402,7 @@ __global__ void mask_ao_kernel(const double* __restrict__ ao, int64_t P, int64_t
   const int64_t k = i % A;
   const int64_t row = i / A;
   const int64_t p = row / 5;
-  out[i] = ao[p * 5 * A + k] == 0.0 ? 0.0 : ao[i];
+  if (QG_STORE_OK(kSiteVjp, i, 5 * P * A)) out[i] = ao[p * 5 * A + k] == 0.0 ? 0.0 : ao[i];
 }
 
 int pick_vjp_level(const AoTables& t, int64_t groups) {
@@ -468,7 +473,8 @@ qmckl_exit_code_device ao_adjoint(Ctx* ctx, qmckl_context_device c, const char* 
     if (t.prim_num > 0) {
       LaunchScope scope(ctx, "vjp_reduce_exponent");
       reduce_alpha_kernel<<<(t.prim_num + 127) / 128, 128, 0, ctx->stream>>>(
-          a.alpha_part, groups, t.prim_num, t.prim_orig, t.prims_unique ? 1 : 0, d_expo_user);
+          a.alpha_part, groups, t.prim_num, t.prim_orig, t.prims_unique ? 1 : 0, d_expo_user,
+          ctx->ao_basis.prim_num);
     }
   }
   if (d_coord_pn) {
@@ -500,6 +506,7 @@ extern "C" {
 qmckl_exit_code_device qmckl_vjp_ao_vgl_device(qmckl_context_device context, const double* ao_vgl_bar,
                                                int64_t ao_vgl_bar_size, double* d_exponent, int64_t d_exponent_size,
                                                double* d_coord, int64_t d_coord_size) {
+  QG_NVTX_RANGE("qmckl_vjp_ao_vgl_device");
   const char* fn = "qmckl_vjp_ao_vgl_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   Ctx* ctx = ctx_of(context);
@@ -547,6 +554,7 @@ qmckl_exit_code_device qmckl_vjp_ao_vgl_device(qmckl_context_device context, con
 qmckl_exit_code_device qmckl_vjp_mo_vgl_device(qmckl_context_device context, const double* w, int64_t w_size,
                                                double* d_coefficient, int64_t d_coefficient_size, double* d_exponent,
                                                int64_t d_exponent_size, double* d_coord, int64_t d_coord_size) {
+  QG_NVTX_RANGE("qmckl_vjp_mo_vgl_device");
   const char* fn = "qmckl_vjp_mo_vgl_device";
   if (qmckl_context_check_device(context) == QMCKL_NULL_CONTEXT_DEVICE) return QMCKL_INVALID_CONTEXT_DEVICE;
   Ctx* ctx = ctx_of(context);

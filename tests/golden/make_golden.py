@@ -105,4 +105,13 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) > 1:
+        main(sys.argv[1])
+    else:
+        sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+        from oracle import oracle
+
+        ref = oracle.reference_dir()
+        if ref is None:
+            sys.exit("reference checkout not found: pass its path or set QMCKL_REFERENCE_DIR")
+        main(ref)

@@ -20,7 +20,7 @@ def setup_module(_):
 def test_library_exports_every_declared_symbol():
     declared = capi.declared_functions()
     assert len(declared) >= 100
-    out = subprocess.check_output(["nm", "-D", "--defined-only", capi.LIB_PATH]).decode()
+    out = subprocess.check_output(["nm", "-D", "--defined-only", capi.lib_path()]).decode()
     exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
     missing = [f for f in declared if f not in exported]
     assert missing == []
@@ -184,6 +184,22 @@ def test_host_allocation_registry():
     assert L.qmckl_free_host(c, p) == 2  # not registered any more
     assert L.qmckl_free_device(c, ctypes.c_void_p(12345)) == 101  # src/qmckl_memory.cpp:201-208
     L.qmckl_context_destroy_device(c)
+
+
+def test_split_wait_test_hook_argument_checks():
+    assert L.qmckl_set_split_wait_test_device(0, 1000, 1) == 103
+    c = L.qmckl_context_create_device(0)
+    assert L.qmckl_set_split_wait_test_device(c, -1, 0) == 2
+    assert L.qmckl_set_split_wait_test_device(c, 1000, 2) == 3
+    assert L.qmckl_set_split_wait_test_device(c, 1000, 1) == 0
+    assert L.qmckl_set_split_wait_test_device(c, 0, 0) == 0
+    L.qmckl_context_destroy_device(c)
+
+
+def test_normal_build_has_no_bounds_checks():
+    assert L.qmckl_bounds_check_status_device(0, None, None, None) == -1
+    assert L.qmckl_bounds_check_selftest_device(5, 4) == -1
+    assert b"bounds-check" not in L.qmckl_gb300_build_info()
 
 
 def test_lock_is_recursive():

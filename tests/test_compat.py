@@ -11,7 +11,11 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_DIR = os.path.join(ROOT, "qmckl_sycl_gb300", "_lib")
-REFERENCE_DIR = "/root/reference"
+
+def _reference_dir():
+    from oracle import oracle
+
+    return oracle.reference_dir()
 
 IDIOM = r'''
 #include "qmckl_gpu_sycl_compat.hpp"
@@ -54,10 +58,12 @@ def test_queue_idiom_compiles_and_links(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE_DIR, "tests")), reason="reference checkout absent")
 def test_reference_test_programs_compile_against_the_c_abi():
+    ref = _reference_dir()
+    if ref is None or not os.path.isdir(os.path.join(ref, "tests")):
+        pytest.skip("reference checkout absent (QMCKL_REFERENCE_DIR)")
     _lib()
-    r = subprocess.run(["sh", os.path.join(ROOT, "oracle", "ref_tests_compile.sh"), REFERENCE_DIR],
+    r = subprocess.run(["sh", os.path.join(ROOT, "oracle", "ref_tests_compile.sh"), ref],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     for t in ("test_qmckl_ao", "test_qmckl_mo"):

@@ -1,0 +1,100 @@
+"""Parity at the full size of the benchmarked workloads, through the C ABI, against the CPU
+oracle over every output value (the reference's own contract for mo_vgl is its golden-file
+check of every value, tests/test_qmckl_mo.cpp:382-405):
+
+- the medium workload (40 nuclei, 600 shells, 1188 AOs, 300 MOs, 256 walkers x 160 electrons =
+  40960 points, seed 0: the bench's system), FP64 form within 1e-12 normwise per vgl component
+  with identical screening (zero) patterns of ao_vgl and ao_value, split-BF16 form within 1e-6
+  normwise per MO component;
+- the batched workload (64 molecules, 5-60 nuclei, 32 walkers x 2N electrons each, about
+  136,000 points), every molecule, both forms, through one batched launch per stage.
+
+The measured maxima are printed (pytest -s shows them)."""
+import numpy as np
+import pytest
+
+from conftest import normwise_rel_err
+from oracle import oracle
+from qmckl_sycl_gb300 import PRECISION_FP64, PRECISION_SPLIT_BF16, Batch, Context, config_batched, config_medium
+
+pytestmark = pytest.mark.gpu
+
+FP64_RTOL = 1e-12
+MIXED_RTOL = 1e-6
+
+
+def per_component(got, ref):
+    return [normwise_rel_err(got[:, c:c + 1], ref[:, c:c + 1]) for c in range(got.shape[1])]
+
+
+@pytest.fixture(scope="module")
+def medium():
+    s = config_medium(0)
+    assert s.point_num == 40960
+    return s, oracle.forward(s, want=("ao_vgl", "ao_value", "mo_vgl", "mo_value"))
+
+
+def test_medium_fp64_every_value(medium):
+    s, ref = medium
+    P = s.point_num
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(PRECISION_FP64)
+        ao = ctx.get_ao_vgl(P)
+        errs = per_component(ao, ref["ao_vgl"])
+        print("medium FP64 ao_vgl normwise per component: " + " ".join("%.2e" % e for e in errs))
+        assert max(errs) <= FP64_RTOL
+        assert np.array_equal(ao == 0.0, ref["ao_vgl"] == 0.0), "ao_vgl screening pattern differs"
+        del ao
+        av = ctx.get_ao_value(P)
+        assert normwise_rel_err(av, ref["ao_value"]) <= FP64_RTOL
+        assert np.array_equal(av == 0.0, ref["ao_value"] == 0.0), "ao_value screening pattern differs"
+        del av
+        mo = ctx.get_mo_vgl(P)
+        errs = per_component(mo, ref["mo_vgl"])
+        print("medium FP64 mo_vgl normwise per component: " + " ".join("%.2e" % e for e in errs))
+        assert max(errs) <= FP64_RTOL
+        assert normwise_rel_err(ctx.get_mo_value(P), ref["mo_value"]) <= FP64_RTOL
+
+
+def test_medium_split_bf16_every_value(medium):
+    s, ref = medium
+    P = s.point_num
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(PRECISION_SPLIT_BF16)
+        mo = ctx.get_mo_vgl(P)
+        errs = per_component(mo, ref["mo_vgl"])
+        absmax = np.abs(mo - ref["mo_vgl"]).max(axis=(0, 2))
+        print("medium split-BF16 mo_vgl vs oracle, normwise per component: %s; max abs: %s" % (
+            " ".join("%.2e" % e for e in errs), " ".join("%.2e" % e for e in absmax)))
+        assert max(errs) <= MIXED_RTOL
+        assert normwise_rel_err(ctx.get_mo_value(P), ref["mo_value"]) <= MIXED_RTOL
+
+
+@pytest.mark.parametrize("mode", [PRECISION_FP64, PRECISION_SPLIT_BF16])
+def test_batched_workload_every_molecule(mode):
+    systems = config_batched(0)
+    assert len(systems) == 64
+    ctxs = []
+    for s in systems:
+        c = Context(0)
+        c.load_system(s)
+        ctxs.append(c)
+    b = Batch(ctxs)
+    try:
+        b.set_precision(mode)
+        outs = b.get_mo_vgl()
+        tol = FP64_RTOL if mode == PRECISION_FP64 else MIXED_RTOL
+        worst = np.zeros(5)
+        for s, got in zip(systems, outs):
+            ref = oracle.forward(s, want=("mo_vgl",))["mo_vgl"]
+            worst = np.maximum(worst, per_component(got, ref))
+        print("batched (%d molecules, %d points) %s mo_vgl worst normwise per component: %s" % (
+            len(systems), sum(s.point_num for s in systems), "FP64" if mode == PRECISION_FP64 else "split-BF16",
+            " ".join("%.2e" % e for e in worst)))
+        assert worst.max() <= tol
+    finally:
+        b.close()
+        for c in ctxs:
+            c.close()

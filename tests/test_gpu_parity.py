@@ -90,6 +90,31 @@ def test_points_far_away_are_screened_to_zero():
     assert np.all(out["ao_vgl"][::2] == 0.0) and np.all(out["mo_vgl"][::2] == 0.0)
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_nan_coordinates_propagate_like_the_reference(mode):
+    # The reference's screening tests are false for a NaN r2, so it screens nothing for a NaN
+    # coordinate and every AO (and hence every MO) of that point is NaN
+    # (src/qmckl_ao_sycl.cpp:53,72-75; src/qmckl_mo_sycl.cpp:40 keeps NaN values); the other
+    # points are unaffected. Both precision forms, and the shell radials' getter.
+    from test_oracle_golden import nan_points
+
+    s = nan_points(config_small(9, point_num=40))
+    ref = oracle.forward(s)
+    ref["shell_vgl"] = oracle.shell_vgl(s)
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(mode)
+        P = s.point_num
+        out = dict(ao_vgl=ctx.get_ao_vgl(P), ao_value=ctx.get_ao_value(P), mo_vgl=ctx.get_mo_vgl(P),
+                   mo_value=ctx.get_mo_value(P), shell_vgl=ctx.get_shell_vgl(P, s.shell_num))
+    for k in out:
+        assert np.array_equal(np.isnan(out[k]), np.isnan(ref[k])), k
+        tol = RTOL if mode == 0 or k in ("ao_vgl", "ao_value", "shell_vgl") else 1e-6
+        assert normwise_rel_err(np.nan_to_num(out[k]), np.nan_to_num(ref[k])) <= tol, k
+    assert np.isnan(out["mo_vgl"][[3, 7, 12]]).all()
+    assert np.array_equal(out["ao_vgl"] == 0.0, ref["ao_vgl"] == 0.0)
+
+
 def test_mo_skips_zero_valued_aos_like_the_reference():
     # A point on the plane x = X_n of a nucleus makes that nucleus' p_x value exactly 0
     # while its x-derivative is not; the reference drops such AOs from the MO sum for all

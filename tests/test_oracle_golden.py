@@ -47,6 +47,31 @@ def test_oracle_bitwise_equal_to_reference(name, chbrclf):
         assert np.array_equal(r[k], o[k]), k
 
 
+def test_oracle_nan_coordinates_equal_to_reference():
+    # NaN coordinates: the reference screens nothing for them (its `>` tests are false for NaN)
+    # and every output of the point is NaN; the oracle must give the same bits elsewhere and
+    # NaN in the same places
+    if oracle.reference_lib() is None:
+        pytest.skip("reference library not built on this machine (needs the reference checkout)")
+    s = nan_points(config_small(9, point_num=40))
+    want = ("ao_vgl", "ao_value", "mo_vgl", "mo_value")
+    r = oracle.reference_forward(s, want=want)
+    o = oracle.forward(s, want=want)
+    for k in want:
+        assert np.array_equal(np.isnan(r[k]), np.isnan(o[k])), k
+        assert np.array_equal(np.nan_to_num(r[k]), np.nan_to_num(o[k])), k
+    assert np.isnan(o["mo_vgl"][7]).all() and not np.isnan(o["mo_vgl"][0]).any()
+
+
+def nan_points(s):
+    """The system with NaN in some coordinates: point 3 (x), point 7 (x, y, z), point 12 (z)."""
+    coord = s.coord.copy()
+    coord[3, 0] = np.nan
+    coord[7, :] = np.nan
+    coord[12, 2] = np.nan
+    return s.with_points(coord)
+
+
 def test_oracle_shell_vgl_matches_reference_layout(chbrclf):
     sv = oracle.shell_vgl(chbrclf)
     assert sv.shape == (chbrclf.point_num, 5, chbrclf.shell_num)
