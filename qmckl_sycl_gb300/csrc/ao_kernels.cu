@@ -297,7 +297,6 @@ struct ShellVals {
   double t1, t2, t3;  // radial gradient = g * (x, y, z)
   double Rt;   // t4 + 2 l g, the radial part of the Laplacian after Euler's identity
   float Rf, t1f, t2f, t3f;  // FP32 copies for the split-BF16 form's value and gradient
-  bool nan;    // NaN radial sums (NaN coordinate): every output of the shell is NaN
 };
 
 // Powers 0..3 of the displacement from the nucleus, FP64 and (split-BF16 form) FP32.
@@ -381,14 +380,9 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
     }
     // the reference's MO kernel skips an AO whose FP64 value P R f is exactly zero
     // (src/qmckl_mo_sycl.cpp:40): decided on the bits of the factors
-    bool drop = zero || (bits_of(P) << 1) == 0 || (bits_of(s.R) << 1) == 0 || (bits_of(f) << 1) == 0;
+    const bool drop = zero || (bits_of(P) << 1) == 0 || (bits_of(s.R) << 1) == 0 || (bits_of(f) << 1) == 0;
     if (zero) v0 = 0.f;
-    float lapf = f64_to_f32(lap);
-    if (s.nan) {  // the FP64 value is NaN (never skipped); the FP32 conversions would give infinities
-      v0 = gx = gy = gz = lapf = __int_as_float(0x7FC00000);
-      drop = false;
-    }
-    w.emit_mixed(v0, gx, gy, gz, lapf, drop);
+    w.emit_mixed(v0, gx, gy, gz, f64_to_f32(lap), drop);
     return;
   }
   const double yz = Y[b] * Z[c];
@@ -533,6 +527,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     // the radial sums of its shells with primitives become NaN below.
     const bool nanr = (r2b << 1) > 0xFFE0000000000000ull;
     const bool scr = r2b > N.screen_bits && !nanr;
+    const bool nan_warp = __any_sync(kFull, nanr);  // warp-uniform: the NaN fix-up below costs a branch
     if (__all_sync(kFull, scr)) {
       w.emit_zeros(N.ao_end - N.ao_begin);
       continue;
@@ -627,9 +622,12 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
           }
         }
       }
+      if (nan_warp) {
+        // every primitive of a NaN lane is NaN in the reference; the outputs follow by arithmetic
+        // (the split-BF16 form's FP32 copies become infinities or NaN, and the contraction NaN)
+        if (nanr && S.prim_end > S.prim_begin) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
+      }
       ShellVals sv;
-      sv.nan = nanr && S.prim_end > S.prim_begin;
-      if (sv.nan) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
       sv.R = t0;
       if constexpr (O == Out::Planes) {
         // FP32 value/gradient inputs; the radial part of the Laplacian stays FP64:
