@@ -524,9 +524,12 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     // A NaN coordinate makes r2 NaN. The reference's screening tests (`r2 > cutoff * range`,
     // `expo * r2 > cutoff`) are false for NaN, so it screens nothing and every primitive gives
     // exp(NaN) = NaN (src/qmckl_ao_sycl.cpp:53,72-75): such a lane is never screened here, and
-    // the radial sums of its shells with primitives become NaN below.
+    // the radial sums of its shells with primitives become NaN below. Screened: screen_bits <
+    // r2b <= bits(+inf), as one unsigned range compare (NaN patterns lie above +inf); written as
+    // `r2b > screen_bits && !nan` the kernel measured 21 % slower (1.20 against 0.99 ms on the
+    // medium workload's planes).
     const bool nanr = (r2b << 1) > 0xFFE0000000000000ull;
-    const bool scr = r2b > N.screen_bits && !nanr;
+    const bool scr = r2b - N.screen_bits - 1ull < 0x7FF0000000000000ull - N.screen_bits;
     const bool nan_warp = __any_sync(kFull, nanr);  // warp-uniform: the NaN fix-up below costs a branch
     if (__all_sync(kFull, scr)) {
       w.emit_zeros(N.ao_end - N.ao_begin);
