@@ -156,6 +156,14 @@ def clock_sampler(gpu):
 
 
 def cpu_model():
+    """The host CPU's model name (lscpu, which also names Arm cores; else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
     try:
         for line in open("/proc/cpuinfo"):
             if line.lower().startswith(("model name", "cpu model")):

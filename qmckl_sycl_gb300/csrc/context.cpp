@@ -249,6 +249,8 @@ qmckl_exit_code_device qmckl_context_destroy_device(const qmckl_context_device c
     cudaEventDestroy(e.stop);
   }
   for (auto e : ctx->event_pool) cudaEventDestroy(e);
+  for (auto e : ctx->chunk_done)
+    if (e) cudaEventDestroy(e);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   cudaGetLastError();

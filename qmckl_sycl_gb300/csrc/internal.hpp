@@ -214,6 +214,26 @@ struct AoBasisData {
   bool provided = false;
 };
 
+// The host-buffer path's contraction jobs (one per point range), kept on the device while the
+// shape and buffers they were encoded for stay the same.
+constexpr int kMaxHostChunks = 16;
+struct HostChunkKey {
+  int64_t P = 0, M = 0, kp = 0;
+  int chunks = 0;
+  double ratio = 0.0;
+  const void *a_planes = nullptr, *b_planes = nullptr, *out = nullptr, *perm = nullptr;
+  bool operator==(const HostChunkKey& o) const {
+    return P == o.P && M == o.M && kp == o.kp && chunks == o.chunks && ratio == o.ratio && a_planes == o.a_planes &&
+           b_planes == o.b_planes && out == o.out && perm == o.perm;
+  }
+};
+struct HostChunkJobs {
+  HostChunkKey key;
+  void* jobs = nullptr;  // device copy of the SplitJob list
+  size_t jobs_cap = 0;
+  int tiles[kMaxHostChunks] = {};
+};
+
 struct MoBasisData {
   int64_t mo_num = 0;
   double* coefficient = nullptr;    // [mo_num][ao_num]
@@ -232,6 +252,7 @@ struct MoBasisData {
   size_t ao_split_cap = 0;
   void* split_job = nullptr;  // device copy of the contraction's job descriptor
   size_t split_job_cap = 0;
+  HostChunkJobs host_jobs;    // the host-buffer path's job list
   int32_t uninitialized = 0;
   bool provided = false;
 };
@@ -260,6 +281,7 @@ struct qmckl_context_struct_device {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   cudaStream_t copy_stream = nullptr;  // device-to-host copies overlapped with compute
+  cudaEvent_t chunk_done[qg::kMaxHostChunks] = {};  // host-buffer path: range k computed
   bool async = false;
   int32_t precision = QMCKL_PRECISION_FP64_DEVICE;
   int32_t shared_exp = QMCKL_SHARED_EXP_AUTO_DEVICE;  // shared exponentials of the AO kernels
@@ -470,7 +492,8 @@ cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, 
 int64_t split_k_pad(int64_t ao_num);
 // mo_vgl of the split-BF16 form computed in `chunks` point ranges whose results are copied to the
 // host buffer while the next range computes (the cache ends up holding the full result).
-qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks);
+qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks,
+                                            double ratio);
 // The member's coefficient planes for the split-BF16 form (built once per coefficient set)
 // and its AO-plane buffer for rows x kp (returns null on allocation failure).
 qmckl_exit_code_device split_prepare_coef(Ctx* ctx, qmckl_context_device c, int64_t kp);

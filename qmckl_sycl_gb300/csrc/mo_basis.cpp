@@ -2,6 +2,8 @@
 // (coefficient transpose, src/qmckl_mo_sycl.cpp:137-189), select_mo (src/qmckl_mo.cpp:31-106)
 // and the provide chain for mo_vgl / mo_value (src/qmckl_mo.cpp:114-453).
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -203,6 +205,23 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
   return QMCKL_SUCCESS_DEVICE;
 }
 
+// Point ranges of the host-buffer path and their growth ratio (a range's copy over the host link
+// should take about as long as the next range's computation: the medium workload computes at
+// ~23.6 M points/s and copies at ~16.1 M points/s, a ratio near 1.45).
+constexpr int kHostChunks = 6;
+constexpr double kHostChunkRatio = 1.0;
+
+// QMCKL_GB300_HOST_CHUNKS="<ranges>[,<ratio>]" overrides the plan (for measurements).
+static void host_chunk_plan_override(int* chunks, double* ratio) {
+  const char* v = getenv("QMCKL_GB300_HOST_CHUNKS");
+  if (!v || !*v) return;
+  int n = 0;
+  double r = 0.0;
+  const int got = sscanf(v, "%d,%lf", &n, &r);
+  if (got >= 1 && n >= 1 && n <= kMaxHostChunks) *chunks = n;
+  if (got == 2 && r >= 1.0 && r <= 4.0) *ratio = r;
+}
+
 // True for host memory (page-locked or not): a destination the device reaches over the host link.
 static bool host_memory(const void* p) {
   cudaPointerAttributes a;
@@ -224,11 +243,13 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
   if (mo.provided && ctx->ao_basis.provided && ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE &&
       ctx->point.date > mo.mo_vgl_date && ctx->point.num >= 16384 && mo_vgl &&
       size_max >= 5 * ctx->point.num * mo.mo_num && ensure_device(ctx) && host_memory(mo_vgl)) {
-    // six chunks: measured on 40960 points (medium workload) 3.67 / 3.37 / 3.21 / 3.13 / 3.10 /
-    // 3.18 ms per step for 2 / 3 / 4 / 5 / 6 / 8 chunks (the ~193 GB/s device-to-host link needs
-    // 2.54 ms for the 491 MB of mo_vgl, the computation 1.83 ms; smaller chunks lose more to kernel
-    // tails than they gain in overlap)
-    qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, 6);
+    // point ranges growing geometrically (QMCKL_GB300_HOST_CHUNKS="<ranges>,<ratio>" overrides the
+    // plan); the device-to-host link (~193 GB/s) needs 2.54 ms for the medium workload's 491 MB of
+    // mo_vgl, the computation 1.73 ms
+    int chunks = kHostChunks;
+    double ratio = kHostChunkRatio;
+    host_chunk_plan_override(&chunks, &ratio);
+    qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, chunks, ratio);
     if (rc != QMCKL_SUCCESS_DEVICE) return rc;
     mo.mo_vgl_date = ctx->date;
     return QMCKL_SUCCESS_DEVICE;

@@ -1017,18 +1017,46 @@ void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
   return ensure_a_planes(ctx, rows, kp) ? ctx->mo_basis.ao_split : nullptr;
 }
 
-// mo_vgl of the split-BF16 form for a caller's host buffer: the points are processed in chunks
-// (contiguous point ranges, each ordered on its own) whose rows of the cached mo_vgl are copied to
-// the host on a second stream while the next chunk computes, so the device-to-host transfer (~190
-// GB/s over the host link here, 2.6 ms for the medium workload's 491 MB) overlaps the compute.
-qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks) {
+// Point ranges of the host-buffer path: growing geometrically by `ratio` from a small first
+// range, so that the copy of each range (at the host link's rate) lasts about as long as the
+// computation of the next one and the link starts early; multiples of 32 points, the last range
+// takes the rest.
+std::vector<int64_t> chunk_plan(int64_t P, int chunks, double ratio) {
+  std::vector<int64_t> sizes;
+  double total = 0.0, w = 1.0;
+  for (int k = 0; k < chunks; ++k, w *= ratio) total += w;
+  int64_t done = 0;
+  w = 1.0;
+  for (int k = 0; k < chunks && done < P; ++k, w *= ratio) {
+    int64_t n = k == chunks - 1 ? P - done : round_up((int64_t)(P * (w / total)), 32);
+    if (n < 32) n = 32;
+    if (n > P - done) n = P - done;
+    sizes.push_back(n);
+    done += n;
+  }
+  return sizes;
+}
+
+// mo_vgl of the split-BF16 form for a caller's host buffer: the points are processed in ranges
+// (contiguous, each ordered on its own) whose rows of the cached mo_vgl are copied to the host on
+// a second stream while the next range computes, so the device-to-host transfer (~193 GB/s over
+// the host link here, 2.54 ms for the medium workload's 491.5 MB, the same for every buffer kind
+// and copy method measured) overlaps the compute. The ranges grow (chunk_plan) so that the link
+// is busy from early on; their contraction jobs are encoded and uploaded once per shape and
+// buffer set, and reused while those stay the same.
+qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks,
+                                            double ratio) {
   const char* fn = "qmckl_get_mo_basis_mo_vgl_device";
   const int64_t P = ctx->point.num, A = ctx->ao_basis.ao_num, M = ctx->mo_basis.mo_num;
   MoBasisData& mo = ctx->mo_basis;
   AoBasisData& ao = ctx->ao_basis;
   const int64_t kp = round_up(A, kBK);
-  chunks = chunks < 1 ? 1 : (chunks > 16 ? 16 : chunks);
-  const int64_t pc = round_up((P + chunks - 1) / chunks, 32);  // points per chunk
+  chunks = chunks < 1 ? 1 : (chunks > kMaxHostChunks ? kMaxHostChunks : chunks);
+  const std::vector<int64_t> sizes = chunk_plan(P, chunks, ratio);
+  const int nc = (int)sizes.size();
+  int64_t pc = 0;  // points of the largest range
+  for (int64_t n : sizes) pc = n > pc ? n : pc;
+  pc = round_up(pc, 32);
   if (5 * pc > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
   qmckl_exit_code_device rc = ensure_tables(ctx, c);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -1053,42 +1081,56 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
     cudaGetLastError();
     return fail(c, QMCKL_FAILURE_DEVICE, fn, "stream creation failed");
   }
-  const int nc = (int)((P + pc - 1) / pc);
-  if (!ensure_raw(ctx, &mo.split_job, &mo.split_job_cap, sizeof(SplitJob) * (size_t)nc))
-    return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptor");
+  for (int k = 0; k < nc; ++k)
+    if (!ctx->chunk_done[k] && cudaEventCreateWithFlags(&ctx->chunk_done[k], cudaEventDisableTiming) != cudaSuccess) {
+      ctx->chunk_done[k] = nullptr;
+      cudaGetLastError();
+      return fail(c, QMCKL_FAILURE_DEVICE, fn, "event creation failed");
+    }
   __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
-  // every chunk's job up front, in one upload: a descriptor copy per chunk from pageable memory
-  // would make the host wait for the stream between chunks
-  std::vector<SplitJob> jobs((size_t)nc);
-  std::vector<int> tiles((size_t)nc);
-  for (int k = 0; k < nc; ++k) {
-    const int64_t off = k * pc, n = P - off < pc ? P - off : pc;
-    tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 32), n, ao.point_perm,
-                           static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
-    if (tiles[k] < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
+  // the ranges' jobs, encoded and uploaded once for this shape and these buffers
+  HostChunkJobs& hj = mo.host_jobs;
+  const HostChunkKey key{P, M, kp, nc, ratio, ap, mo.coef_split, mo.mo_vgl, ao.point_perm};
+  if (!(hj.key == key) || !hj.jobs) {
+    hj.key = HostChunkKey{};
+    if (!ensure_raw(ctx, &hj.jobs, &hj.jobs_cap, sizeof(SplitJob) * (size_t)nc))
+      return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptors");
+    std::vector<SplitJob> jobs((size_t)nc);
+    int64_t off = 0;
+    for (int k = 0; k < nc; ++k) {
+      const int64_t n = sizes[k];
+      hj.tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 32), n, ao.point_perm,
+                                static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
+      if (hj.tiles[k] < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
+      off += n;
+    }
+    if (cudaMemcpy(hj.jobs, jobs.data(), sizeof(SplitJob) * (size_t)nc, cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, QMCKL_FAILURE_DEVICE, fn, "job upload failed");
+    }
+    hj.key = key;
   }
-  SplitJob* d_jobs = static_cast<SplitJob*>(mo.split_job);
-  cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SplitJob) * (size_t)nc, cudaMemcpyHostToDevice,
-                                  ctx->stream);
-  cudaEvent_t done[16];
-  for (int k = 0; k < nc; ++k) cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+  const SplitJob* d_jobs = static_cast<const SplitJob*>(hj.jobs);
+  cudaError_t e = cudaSuccess;
+  int64_t off = 0;
   for (int k = 0; k < nc && e == cudaSuccess; ++k) {
-    const int64_t off = k * pc, n = P - off < pc ? P - off : pc;
+    const int64_t n = sizes[k];
     const double* coord = ctx->point.coord + off;  // rows of [3][P], slice of n points
     launch_point_order(ctx, ao.tables, coord, P, n, ao.point_keys, ao.cell_counts, ao.point_perm);
     launch_ao_planes(ctx, ao.tables, coord, P, ao.point_perm, n, kp, ap);
     {
       LaunchScope scope(ctx, "mo_vgl_split_bf16");
-      launch_split_jobs(ctx->stream, d_jobs + k, 1, tiles[k], err, ctl_of(ctx));
+      e = launch_split_jobs(ctx->stream, d_jobs + k, 1, hj.tiles[k], err, ctl_of(ctx));
     }
-    cudaEventRecord(done[k], ctx->stream);
-    cudaStreamWaitEvent(ctx->copy_stream, done[k], 0);
-    e = cudaMemcpyAsync(host_dst + 5 * off * M, mo.mo_vgl + 5 * off * M, sizeof(double) * 5 * n * M,
-                        cudaMemcpyDeviceToHost, ctx->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->chunk_done[k], ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[k], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(host_dst + 5 * off * M, mo.mo_vgl + 5 * off * M, sizeof(double) * 5 * n * M,
+                          cudaMemcpyDeviceToHost, ctx->copy_stream);
+    off += n;
   }
   cudaError_t e2 = cudaStreamSynchronize(ctx->copy_stream);
   cudaError_t e3 = cudaStreamSynchronize(ctx->stream);
-  for (int k = 0; k < nc; ++k) cudaEventDestroy(done[k]);
   if (e == cudaSuccess) e = e2 != cudaSuccess ? e2 : e3;
   if (e != cudaSuccess) {
     cudaGetLastError();
