@@ -219,7 +219,7 @@ static void host_chunk_plan_override(int* chunks, double* ratio) {
   double r = 0.0;
   const int got = sscanf(v, "%d,%lf", &n, &r);
   if (got >= 1 && n >= 1 && n <= kMaxHostChunks) *chunks = n;
-  if (got == 2 && r >= 1.0 && r <= 4.0) *ratio = r;
+  if (got == 2 && r >= 0.25 && r <= 4.0) *ratio = r;
 }
 
 // True for host memory (page-locked or not): a destination the device reaches over the host link.
