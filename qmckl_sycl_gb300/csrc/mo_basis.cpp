@@ -205,9 +205,12 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
   return QMCKL_SUCCESS_DEVICE;
 }
 
-// Point ranges of the host-buffer path and their growth ratio (a range's copy over the host link
-// should take about as long as the next range's computation: the medium workload computes at
-// ~23.6 M points/s and copies at ~16.1 M points/s, a ratio near 1.45).
+// Point ranges of the host-buffer path and their size ratio (1: equal ranges). Measured end to
+// end on the medium workload (set_point from and mo_vgl into page-locked host memory, ms per
+// step): 6 equal ranges 3.01, 5 3.13, 7 3.02, 8 2.98, 10 3.32; ranges growing by 1.15 / 1.45 per
+// range (a small first range starts the link early) 3.06 / 3.38, shrinking by 0.85 / 0.7 3.16 /
+// 3.32. The small ranges' kernels run far below the full-size rates, which costs more than the
+// earlier start of the copies gains.
 constexpr int kHostChunks = 6;
 constexpr double kHostChunkRatio = 1.0;
 
@@ -243,9 +246,9 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
   if (mo.provided && ctx->ao_basis.provided && ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE &&
       ctx->point.date > mo.mo_vgl_date && ctx->point.num >= 16384 && mo_vgl &&
       size_max >= 5 * ctx->point.num * mo.mo_num && ensure_device(ctx) && host_memory(mo_vgl)) {
-    // point ranges growing geometrically (QMCKL_GB300_HOST_CHUNKS="<ranges>,<ratio>" overrides the
-    // plan); the device-to-host link (~193 GB/s) needs 2.54 ms for the medium workload's 491 MB of
-    // mo_vgl, the computation 1.73 ms
+    // equal point ranges (QMCKL_GB300_HOST_CHUNKS="<ranges>,<ratio>" overrides the plan); the
+    // device-to-host link (~193 GB/s) needs 2.54 ms for the medium workload's 491 MB of mo_vgl,
+    // the computation 1.73 ms
     int chunks = kHostChunks;
     double ratio = kHostChunkRatio;
     host_chunk_plan_override(&chunks, &ratio);

@@ -1017,10 +1017,8 @@ void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
   return ensure_a_planes(ctx, rows, kp) ? ctx->mo_basis.ao_split : nullptr;
 }
 
-// Point ranges of the host-buffer path: growing geometrically by `ratio` from a small first
-// range, so that the copy of each range (at the host link's rate) lasts about as long as the
-// computation of the next one and the link starts early; multiples of 32 points, the last range
-// takes the rest.
+// Point ranges of the host-buffer path: sizes in the ratio 1 : ratio : ratio^2 ... (ratio 1: equal
+// ranges), multiples of 32 points, the last range taking the rest.
 std::vector<int64_t> chunk_plan(int64_t P, int chunks, double ratio) {
   std::vector<int64_t> sizes;
   double total = 0.0, w = 1.0;
@@ -1041,9 +1039,8 @@ std::vector<int64_t> chunk_plan(int64_t P, int chunks, double ratio) {
 // (contiguous, each ordered on its own) whose rows of the cached mo_vgl are copied to the host on
 // a second stream while the next range computes, so the device-to-host transfer (~193 GB/s over
 // the host link here, 2.54 ms for the medium workload's 491.5 MB, the same for every buffer kind
-// and copy method measured) overlaps the compute. The ranges grow (chunk_plan) so that the link
-// is busy from early on; their contraction jobs are encoded and uploaded once per shape and
-// buffer set, and reused while those stay the same.
+// and copy method measured) overlaps the compute. The ranges' contraction jobs are encoded and
+// uploaded once per shape and buffer set, and reused while those stay the same.
 qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks,
                                             double ratio) {
   const char* fn = "qmckl_get_mo_basis_mo_vgl_device";
