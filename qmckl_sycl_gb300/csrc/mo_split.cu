@@ -67,6 +67,11 @@ constexpr uint32_t kMaxStage = 3 * kPlaneA + 3 * (uint32_t)kMaxN * kBK * 2;  // 
 constexpr int kTPitch = 9;                   // transposition buffer: 32 rows x 8 floats, row pitch 9
 constexpr uint32_t kTBuf = 32 * kTPitch * 4;  // bytes per fold warp
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
+#ifndef QMCKL_SPLIT_TWO_SUM
+#define QMCKL_SPLIT_TWO_SUM 1
+#endif
+// The fold keeps the running main product as an FP32 two-sum (hi, lo); without it, as one FP32 sum.
+constexpr bool kTwoSum = QMCKL_SPLIT_TWO_SUM != 0;
 
 // Launch controls of the contraction kernel: the limit of every mbarrier wait (clock cycles),
 // and, for the failure-handling test only, a producer that issues no loads, so that the
@@ -475,12 +480,14 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
             const f32x2 v = pack2(rv[q], rv[q + 1]);
             if (kb == 0) {
               h2[i] = v;
-              l2[i] = 0ull;
-            } else {
+              if constexpr (kTwoSum) l2[i] = 0ull;
+            } else if constexpr (kTwoSum) {
               f32x2 s2, e2;
               two_sum2(h2[i], v, s2, e2);
               h2[i] = s2;
               l2[i] = add2(l2[i], e2);
+            } else {
+              h2[i] = add2(h2[i], v);
             }
           }
         }
@@ -501,9 +508,13 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
       for (int q = 0; q < 16; q += 2) {
         if (q < 8 || full16) {
           const int i = (c0 + q) >> 1;
-          f32x2 s2, e2;
-          two_sum2(h2[i], pack2(rc[q], rc[q + 1]), s2, e2);
-          h2[i] = add2(s2, add2(l2[i], e2));  // hi + (lo + e) rounded once to FP32 (2^-24 relative)
+          if constexpr (kTwoSum) {
+            f32x2 s2, e2;
+            two_sum2(h2[i], pack2(rc[q], rc[q + 1]), s2, e2);
+            h2[i] = add2(s2, add2(l2[i], e2));  // hi + (lo + e) rounded once to FP32 (2^-24 relative)
+          } else {
+            h2[i] = add2(h2[i], pack2(rc[q], rc[q + 1]));
+          }
         }
       }
     }
