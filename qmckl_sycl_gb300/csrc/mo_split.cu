@@ -20,9 +20,12 @@
 // its largest product). The five correction products (all ~2^-8 of the result or smaller)
 // go into their own accumulator; the main hi*hi product is accumulated for two 64-wide K
 // blocks at a time (eight MMAs) in one of two alternating tensor-memory buffers, and the fold
-// warps add each finished block sum into a running FP32 two-sum (hi, lo) held in registers
-// while the next blocks are multiplied. The error therefore does not grow with K. The result
-// is hi + (lo + corrections), rounded once to FP32 and widened exactly to FP64.
+// warps add each finished block sum into a running FP32 sum held in registers (rounded, not
+// truncated) while the next blocks are multiplied, so the truncation error does not grow with K.
+// The result is that sum + corrections, rounded once to FP32 and widened exactly to FP64. (A
+// compensated FP32 two-sum (hi, lo) for the running sum, QMCKL_SPLIT_TWO_SUM=1, lowers the
+// medium workload's worst normwise error from 5.1e-7 to 4.9e-7 and costs 5 % of the contraction
+// there, 16 % on the 64-molecule batch: measured 0.655 / 0.691 ms and 1.627 / 1.946 ms.)
 //
 // GEMM structure (persistent, one CTA per SM, 128 x N output tiles with N <= 160): warp 0
 // issues TMA loads of the six operand planes per 64-wide K block into a two-stage ring of
@@ -54,7 +57,7 @@ constexpr int kMaxN = 160;      // columns per tile: two halves of <= 80, each f
 constexpr int kHalfN = kMaxN / 2;
 constexpr int kThreads = 384;   // 12 warps = 3 warpgroups: {TMA, MMA, 2 idle}, 8 fold warps
 constexpr int kBufs = 2;         // main-product TMEM buffers: the MMAs run up to one fold group ahead
-constexpr int kFold = 2;         // K blocks (of 64) per main-product block sum folded into the two-sum
+constexpr int kFold = 2;         // K blocks (of 64) per main-product block sum folded into the running sum
 // Tensor memory (512 columns): corrections [0, kMaxN), main buffer b at kMaxN * (1 + b).
 static_assert(kMaxN * (1 + kBufs) <= 512, "tensor memory holds the corrections and the main buffers");
 // registers per thread after setmaxnreg: warpgroup 0 (TMA, MMA), warpgroups 1 and 2 (fold);
@@ -68,9 +71,10 @@ constexpr int kTPitch = 9;                   // transposition buffer: 32 rows x 
 constexpr uint32_t kTBuf = 32 * kTPitch * 4;  // bytes per fold warp
 constexpr long long kWaitCycles = 2000000000LL;  // ~1 s at GB300 clocks
 #ifndef QMCKL_SPLIT_TWO_SUM
-#define QMCKL_SPLIT_TWO_SUM 1
+#define QMCKL_SPLIT_TWO_SUM 0
 #endif
-// The fold keeps the running main product as an FP32 two-sum (hi, lo); without it, as one FP32 sum.
+// The fold keeps the running main product as one FP32 sum, or (QMCKL_SPLIT_TWO_SUM=1) as an FP32
+// two-sum (hi, lo).
 constexpr bool kTwoSum = QMCKL_SPLIT_TWO_SUM != 0;
 
 // Launch controls of the contraction kernel: the limit of every mbarrier wait (clock cycles),
@@ -434,15 +438,15 @@ __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, bool full16, uint32
 
 // One fold warp's work on one tile (one row per thread, this warp's half of the N columns):
 // after every kFold K blocks, the main product's FP32 block sum is read out of tensor memory and
-// added into a running two-sum (hi, lo) held in registers (tensor-memory traffic slows the MMAs
-// that share it, so the two-sum does not live there); at the end hi + (lo + corrections) is
-// formed, tensor memory is released to the next tile, and the warp writes its 32 x N/2 block of
+// added into a running sum held in registers (tensor-memory traffic slows the MMAs that share it,
+// so the sum does not live there); at the end sum + corrections is formed, tensor memory is released to the next tile, and the warp writes its 32 x N/2 block of
 // the output: with 32-byte stores of each lane's own row where the rows allow it, otherwise eight
 // columns at a time through the transposition buffer (each store instruction then writes four
 // rows x 64 contiguous bytes). it: the running fold-group index (advanced). Returns false when a
 // wait gave up.
 __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job, const TileRef& tr, uint32_t& it) {
-  // running two-sum of the main product, two columns per register: hi in h2, lo in l2
+  // running sum of the main product, two columns per register, in h2 (and its two-sum's low part
+  // in l2 when kTwoSum)
   f32x2 h2[kHalfN / 2], l2[kHalfN / 2];
   const int nh = job.n_tile >> 1;             // columns of this warp: [hc, hc + nh)
   const uint32_t hc = (uint32_t)(f.half * nh);
