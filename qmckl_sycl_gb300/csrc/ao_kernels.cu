@@ -47,6 +47,11 @@ namespace qg {
 namespace {
 
 constexpr int kWarps = 4;          // warps per CTA (each runs its own task)
+#ifndef QMCKL_AO_TASKS_PER_WARP
+#define QMCKL_AO_TASKS_PER_WARP 2
+#endif
+// Tasks per resident warp the nucleus-chunk level is chosen for (finer chunks give more tasks).
+constexpr int kTasksPerWarp = QMCKL_AO_TASKS_PER_WARP;
 using namespace dev;
 
 enum class Out { Vgl, Value, Planes };
@@ -912,7 +917,7 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
   // two or more tasks per resident warp, taken from a counter: with one task per warp the SMs
   // that receive one CTA more than the others set the time (4 or 5 CTAs per SM on the medium
   // workload, 16 % idle FP64 issue)
-  FusedArgs a = make_fused_args(t, pick_level(t, groups, 2 * resident_warps), coord, perm, point_num, out, planes,
+  FusedArgs a = make_fused_args(t, pick_level(t, groups, kTasksPerWarp * resident_warps), coord, perm, point_num, out, planes,
                                 row_len);
   if (coord_ld >= 0) a.coord_ld = coord_ld;
   a.ent = B ? t.ent : nullptr;
