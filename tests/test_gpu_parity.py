@@ -117,6 +117,36 @@ def test_nan_coordinates_propagate_like_the_reference(mode):
     assert np.array_equal(out["ao_vgl"] == 0.0, ref["ao_vgl"] == 0.0)
 
 
+def _g_shells():
+    # angular momenta up to 5: the fused kernels' generic (run-time exponent) path. The reference
+    # built on the host corrupts its heap on l >= 4 inputs, so the oracle alone pins this case.
+    from qmckl_sycl_gb300.systems import make_system
+
+    return make_system(11, 5, 8, 5.0, 40, (0.3, 0.2, 0.2, 0.1, 0.1, 0.1), 4, (0.1, 20.0), 30, 96, 1.5, name="g")
+
+
+@pytest.mark.parametrize("name", ["g_shells", "g_shells_nan", "zero_prim", "zero_prim_nan"])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_high_l_and_zero_primitive_shells(name, mode):
+    from test_oracle_golden import nan_points, zero_prim_shells
+
+    s = _g_shells() if name.startswith("g_shells") else zero_prim_shells(config_small(12, point_num=64))
+    if name.endswith("_nan"):
+        s = nan_points(s)
+    ref = oracle.forward(s)
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(mode)
+        P = s.point_num
+        out = dict(ao_vgl=ctx.get_ao_vgl(P), ao_value=ctx.get_ao_value(P), mo_vgl=ctx.get_mo_vgl(P),
+                   mo_value=ctx.get_mo_value(P))
+    for k in out:
+        assert np.array_equal(np.isnan(out[k]), np.isnan(ref[k])), k
+        tol = RTOL if mode == 0 or k.startswith("ao") else 1e-6
+        assert normwise_rel_err(np.nan_to_num(out[k]), np.nan_to_num(ref[k])) <= tol, (k, name)
+    assert np.array_equal(out["ao_vgl"] == 0.0, ref["ao_vgl"] == 0.0)
+
+
 def test_mo_skips_zero_valued_aos_like_the_reference():
     # A point on the plane x = X_n of a nucleus makes that nucleus' p_x value exactly 0
     # while its x-derivative is not; the reference drops such AOs from the MO sum for all

@@ -63,6 +63,30 @@ def test_oracle_nan_coordinates_equal_to_reference():
     assert np.isnan(o["mo_vgl"][7]).all() and not np.isnan(o["mo_vgl"][0]).any()
 
 
+def zero_prim_shells(s, shells=(3, 10, 25)):
+    """The system with some shells given no primitives (their radial sums are zero)."""
+    spn = s.shell_prim_num.copy()
+    spn[list(shells)] = 0
+    return s.__class__(**{**s.__dict__, "shell_prim_num": spn})
+
+
+@pytest.mark.parametrize("with_nan", [False, True])
+def test_oracle_zero_primitive_shells_equal_to_reference(with_nan):
+    # shells without primitives contribute zero radials; with NaN coordinates their AOs are 0 or
+    # NaN depending on the polynomial's factors, like the reference's
+    if oracle.reference_lib() is None:
+        pytest.skip("reference library not built on this machine (needs the reference checkout)")
+    s = zero_prim_shells(config_small(12, point_num=64))
+    if with_nan:
+        s = nan_points(s)
+    want = ("ao_vgl", "ao_value", "mo_vgl", "mo_value")
+    r = oracle.reference_forward(s, want=want)
+    o = oracle.forward(s, want=want)
+    for k in want:
+        assert np.array_equal(np.isnan(r[k]), np.isnan(o[k])), k
+        assert np.array_equal(np.nan_to_num(r[k]), np.nan_to_num(o[k])), k
+
+
 def nan_points(s):
     """The system with NaN in some coordinates: point 3 (x), point 7 (x, y, z), point 12 (z)."""
     coord = s.coord.copy()
