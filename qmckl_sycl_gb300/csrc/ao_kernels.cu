@@ -656,6 +656,9 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
         sv.t1 = g * x;
         sv.t2 = g * y;
         sv.t3 = g * z;
+        // a shell without primitives has a zero radial gradient in the reference, also at a NaN
+        // coordinate (where g * x would be NaN)
+        if (nan_warp && nanr && S.prim_end == S.prim_begin) sv.t1 = sv.t2 = sv.t3 = 0.0;
         const double t4 = fma(-2.0, h, 3.0 * g);
         sv.Rt = fma(kTwoL[S.l], g, t4);
       } else {
