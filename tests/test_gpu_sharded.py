@@ -4,7 +4,7 @@ by a gloo process group on 127.0.0.1: each rank evaluates its contiguous range o
 workload's points through its own context. The ranks' mo_vgl rows together must equal a single
 context's bit for bit (points are independent; both forms), and the sharded VJP (one all-reduce of
 the coefficient and exponent gradients, coordinates local) must match the single context's
-gradients within 1e-12 (only the order of the sums over points differs)."""
+gradients within 1e-12 (only the order of some sums differs)."""
 import multiprocessing as mp
 import os
 import socket
@@ -86,8 +86,9 @@ def test_two_ranks_equal_one_context():
     for mode in (0, 1):
         rows = np.concatenate([out[r]["mo_vgl%d" % mode] for r in (0, 1)])
         assert np.array_equal(rows, want[mode]), mode
+    # a point's coordinate gradient sums its nucleus chunks, whose size follows the point count
     coord = np.concatenate([out[r]["grad"]["coord"] for r in (0, 1)])
-    assert np.array_equal(coord, g["coord"])
+    assert normwise_rel_err(coord, g["coord"]) <= 1e-12
     for r in (0, 1):
         for k in ("coef", "expo"):
             assert normwise_rel_err(out[r]["grad"][k], g[k]) <= 1e-12, (r, k)
