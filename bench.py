@@ -109,6 +109,7 @@ class NvmlSampler:
                 return
             self.h = ctypes.c_void_p()
             if self.nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu), ctypes.byref(self.h)) != 0:
+                self.nv.nvmlShutdown()
                 return
             m = ctypes.c_uint()
             if self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(m)) == 0:
@@ -141,6 +142,8 @@ class NvmlSampler:
         if self.ok:
             self.stop = True
             self.t.join()
+            self.nv.nvmlShutdown()  # balances the nvmlInit of this sampler
+            self.ok = False
 
     def summary(self):
         if not self.samples:
@@ -151,6 +154,7 @@ class NvmlSampler:
 
 
 def clock_sampler(gpu):
+    """NVML sampling where the driver's library loads, else nvidia-smi."""
     s = NvmlSampler(gpu)
     return s if s.ok else ClockSampler(gpu)
 

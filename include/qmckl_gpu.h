@@ -537,7 +537,8 @@ qmckl_exit_code_device qmckl_set_split_wait_test_device(qmckl_context_device con
  * 6 split planes, 7 FP64 contraction output, 8 split-K sums, 9 distances, 10 transposes and
  * copies, 11 adjoint), index and extent (elements) when a store was out of range on the current
  * device, 0 when none was, -1 for the normal build (no checks) and -2 on a CUDA error; reset = 1
- * clears the records. Any pointer may be NULL. */
+ * clears the records. It waits for all work on the current device first. Any pointer may be
+ * NULL. */
 int32_t qmckl_bounds_check_status_device(int32_t reset, int64_t* site, int64_t* index, int64_t* extent);
 /* Self-test of that recording: a one-thread kernel evaluates the check for element `index` of an
  * array of `extent` elements (site 10) and stores nothing. Returns 0 when it ran, -1 for the normal

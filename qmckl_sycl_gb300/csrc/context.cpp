@@ -181,6 +181,9 @@ int32_t bounds_check_status(bool reset, int64_t* site, int64_t* index, int64_t* 
     int hit, site;
     long long index, extent;
   };
+  // the records are read once every kernel of every stream (contexts' streams do not
+  // synchronise with the legacy stream that cudaMemcpy uses) has finished
+  if (cudaDeviceSynchronize() != cudaSuccess) return -2;
   int32_t found = 0;
   for (auto address : bounds_records()) {
     void* p = address();
