@@ -52,6 +52,12 @@ constexpr int kWarps = 4;          // warps per CTA (each runs its own task)
 #endif
 // Tasks per resident warp the nucleus-chunk level is chosen for (finer chunks give more tasks).
 constexpr int kTasksPerWarp = QMCKL_AO_TASKS_PER_WARP;
+#ifndef QMCKL_AO_FINE_TAIL
+#define QMCKL_AO_FINE_TAIL 1
+#endif
+// The last tasks of a launch are split this many levels finer (0: not at all). Measured on the
+// medium workload's planes kernel: 0.997 / 0.991 / 0.993 / 0.991 ms for 0 / 1 / 2 / 3 levels.
+constexpr int kFineTailLevels = QMCKL_AO_FINE_TAIL;
 using namespace dev;
 
 enum class Out { Vgl, Value, Planes };
@@ -508,8 +514,17 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
                                         const double* __restrict__ thi, const double* __restrict__ tlo,
                                         const double* __restrict__ fine, double* __restrict__ ebuf, int lane) {
   constexpr int NC = ncomp<O>();
-  const int64_t group = task / a.chunk_num;
-  const int ch = (int)(task - group * a.chunk_num);
+  int64_t group;
+  const NucleusChunk* chunk;
+  if (task < a.tail_task) {
+    group = task / a.chunk_num;
+    chunk = a.chunks + (task - group * a.chunk_num);
+  } else {  // the finer tail
+    const int64_t t = task - a.tail_task;
+    const int64_t g = t / a.tail_chunk_num;
+    group = a.tail_group + g;
+    chunk = a.tail_chunks + (t - g * a.tail_chunk_num);
+  }
   const int64_t p0 = group * 32;
   const int64_t remaining = a.point_num - p0;
   const int nvalid = remaining < 32 ? (int)remaining : 32;
@@ -517,7 +532,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   const int64_t p = a.perm ? (int64_t)a.perm[slot] : slot;
   const double ex = a.coord[p], ey = a.coord[a.coord_ld + p], ez = a.coord[2 * a.coord_ld + p];
 
-  const NucleusChunk cj = a.chunks[ch];
+  const NucleusChunk cj = *chunk;
   Writer<O> w;
   w.init(a, st, p0, lane, nvalid, p, cj.ao_begin);
 
@@ -920,8 +935,11 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
   // two or more tasks per resident warp, taken from a counter: with one task per warp the SMs
   // that receive one CTA more than the others set the time (4 or 5 CTAs per SM on the medium
   // workload, 16 % idle FP64 issue)
-  FusedArgs a = make_fused_args(t, pick_level(t, groups, kTasksPerWarp * resident_warps), coord, perm, point_num, out, planes,
-                                row_len);
+  const int level = pick_level(t, groups, kTasksPerWarp * resident_warps);
+  FusedArgs a = make_fused_args(t, level, coord, perm, point_num, out, planes, row_len);
+  // the last tasks at a finer level: a warp's last task is short, so the launch ends with every
+  // warp busy nearly to the end (a task at the coarse level takes ~1/3 of the launch)
+  if (kFineTailLevels > 0) set_fine_tail(a, t, level + kFineTailLevels, resident_warps);
   if (coord_ld >= 0) a.coord_ld = coord_ld;
   a.ent = B ? t.ent : nullptr;
   a.ent_cap = B ? t.ent_cap : 0;
@@ -1045,7 +1063,26 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.plane_pp = (point_num + 31) / 32 * 32;
   a.coord_ld = point_num;
   a.task_num = ((point_num + 31) / 32) * a.chunk_num;
+  a.tail_chunks = a.chunks;
+  a.tail_chunk_num = a.chunk_num;
+  a.tail_group = (point_num + 31) / 32;
+  a.tail_task = a.task_num;
   return a;
+}
+
+void set_fine_tail(FusedArgs& a, const AoTables& t, int fine, int64_t tail_tasks) {
+  if (fine <= 0 || fine >= (int)t.level_offsets.size()) return;
+  const int n = t.level_sizes[fine];
+  if (n <= a.chunk_num) return;
+  const int64_t groups = (a.point_num + 31) / 32;
+  int64_t tg = (tail_tasks + n - 1) / n;
+  if (tg > groups / 2) tg = groups / 2;
+  if (tg <= 0) return;
+  a.tail_group = groups - tg;
+  a.tail_task = a.tail_group * a.chunk_num;
+  a.tail_chunks = t.chunks + t.level_offsets[fine];
+  a.tail_chunk_num = n;
+  a.task_num = a.tail_task + tg * n;
 }
 
 template <Out O, bool G, bool B>

@@ -431,6 +431,13 @@ struct FusedArgs {
   int64_t coord_ld;         // row stride of coord (point_num, or more for a slice of a larger set)
   int64_t task_num;
   int chunk_num;
+  // Finer tasks at the end: point groups from tail_group on are split at a finer nucleus-chunk
+  // level (tail_chunks, tail_chunk_num chunks), numbered from tail_task = tail_group * chunk_num,
+  // so that the last tasks the warps take are short. tail_task == task_num: no such groups.
+  const NucleusChunk* tail_chunks;
+  int64_t tail_group;
+  int64_t tail_task;
+  int tail_chunk_num;
 };
 // Number of nucleus-chunk levels of the tables (level v has about 2^v chunks).
 int ao_level_count(const AoTables& t);
@@ -440,6 +447,9 @@ int ao_level_count(const AoTables& t);
 bool ao_shared_exponentials(const AoTables& t, bool planes);
 FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
                           double* out, void* planes, int64_t row_len);
+// Splits the last point groups of a at the finer nucleus-chunk level `fine` (about tail_tasks
+// tasks, at most half of the groups; nothing when that level is not finer than a's).
+void set_fine_tail(FusedArgs& a, const AoTables& t, int fine, int64_t tail_tasks);
 // Persistent AO kernel over the tasks of nmol molecules: mols[m]'s tasks are numbered from
 // task_begin[m] (non-decreasing, task_begin[nmol] = total); warps take tasks from *counter
 // (zeroed before the launch). planes selects the BF16-plane output; high_l must be set when
