@@ -100,13 +100,17 @@ __device__ __forceinline__ void dgemm_warp_tile(const double* __restrict__ A, in
     }
 }
 
+// CTA (x, y) covers column block x and row blocks y, y + gridDim.y, ... (gridDim.y is capped at
+// 65535, so more row blocks are walked in turn).
 template <bool MASK>
 __global__ void __launch_bounds__(128) dgemm_dmma_kernel(const double* __restrict__ A, const double* __restrict__ B,
                                                          double* __restrict__ C, int64_t R, int64_t K, int64_t N) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
   const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
-  dgemm_warp_tile<MASK>(A, K, B, C, R, K, N, r0, c0, lane);
+  for (int64_t rb = blockIdx.y; rb * kCM < R; rb += gridDim.y) {
+    const int64_t r0 = rb * kCM + (warp >> 1) * kWM;
+    dgemm_warp_tile<MASK>(A, K, B, C, R, K, N, r0, c0, lane);
+  }
 }
 
 // Split-K: CTA z computes the K-slice [z*kc, min(K, (z+1)*kc)) of A*B into parts[z] (R x N).
@@ -116,9 +120,11 @@ __global__ void __launch_bounds__(128) dgemm_splitk_kernel(const double* __restr
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t k0 = (int64_t)blockIdx.z * kc;
   const int64_t kn = (K - k0) < kc ? (K - k0) : kc;
-  const int64_t r0 = (int64_t)blockIdx.y * kCM + (warp >> 1) * kWM;
   const int64_t c0 = (int64_t)blockIdx.x * kCN + (warp & 1) * kWN;
-  dgemm_warp_tile<false>(A + k0, K, B + k0 * N, parts + (int64_t)blockIdx.z * R * N, R, kn, N, r0, c0, lane);
+  for (int64_t rb = blockIdx.y; rb * kCM < R; rb += gridDim.y) {
+    const int64_t r0 = rb * kCM + (warp >> 1) * kWM;
+    dgemm_warp_tile<false>(A + k0, K, B + k0 * N, parts + (int64_t)blockIdx.z * R * N, R, kn, N, r0, c0, lane);
+  }
 }
 
 // out[i] = sum over z (in order) of parts[z][i].
@@ -173,12 +179,18 @@ cudaError_t launch_batch_shape(cudaStream_t stream, const GemmJob* jobs, const i
   return cudaGetLastError();
 }
 
+// Row blocks of R rows for gridDim.y (at most 65535; the kernels walk the rest).
+int64_t grid_rows(int64_t R) {
+  const int64_t rb = (R + kCM - 1) / kCM;
+  return rb < 65535 ? rb : 65535;
+}
+
 template <bool MASK>
 cudaError_t launch_dgemm(Ctx* ctx, const double* A, const double* B, double* C, int64_t R, int64_t K, int64_t N,
                          const char* name) {
   if (R <= 0 || N <= 0) return cudaSuccess;
   if (K <= 0) return cudaMemsetAsync(C, 0, sizeof(double) * R * N, ctx->stream);
-  dim3 grid((unsigned)((N + kCN - 1) / kCN), (unsigned)((R + kCM - 1) / kCM));
+  dim3 grid((unsigned)((N + kCN - 1) / kCN), (unsigned)grid_rows(R));
   LaunchScope scope(ctx, name);
   dgemm_dmma_kernel<MASK><<<grid, 128, 0, ctx->stream>>>(A, B, C, R, K, N);
   return cudaGetLastError();
@@ -225,7 +237,7 @@ cudaError_t launch_dgemm_splitk(Ctx* ctx, const double* A, const double* B, doub
   int64_t kc = (K + nparts - 1) / nparts;
   kc = (kc + 3) / 4 * 4;
   const int64_t z = (K + kc - 1) / kc;
-  dim3 grid((unsigned)((N + kCN - 1) / kCN), (unsigned)((R + kCM - 1) / kCM), (unsigned)z);
+  dim3 grid((unsigned)((N + kCN - 1) / kCN), (unsigned)grid_rows(R), (unsigned)z);
   {
     LaunchScope scope(ctx, name);
     dgemm_splitk_kernel<<<grid, 128, 0, ctx->stream>>>(A, B, parts, R, K, N, kc);

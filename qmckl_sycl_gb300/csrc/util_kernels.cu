@@ -11,19 +11,23 @@
 namespace qg {
 namespace {
 
-// out[c][r] = in[r][c]; in is rows x cols, C order.
+// out[c][r] = in[r][c]; in is rows x cols, C order. CTA (x, y) transposes column block x of row
+// blocks y, y + gridDim.y, ... (gridDim.y is capped at 65535).
 __global__ void transpose_kernel(const double* __restrict__ in, int64_t rows, int64_t cols, double* __restrict__ out) {
   __shared__ double tile[32][33];
-  const int64_t bx = (int64_t)blockIdx.x * 32, by = (int64_t)blockIdx.y * 32;
-  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-    const int64_t r = by + i, c = bx + threadIdx.x;
-    if (r < rows && c < cols) tile[i][threadIdx.x] = in[r * cols + c];
-  }
-  __syncthreads();
-  for (int i = threadIdx.y; i < 32; i += blockDim.y) {
-    const int64_t c = bx + i, r = by + threadIdx.x;
-    if (c < cols && r < rows && QG_STORE_OK(kSiteUtil, c * rows + r, rows * cols))
-      out[c * rows + r] = tile[threadIdx.x][i];
+  const int64_t bx = (int64_t)blockIdx.x * 32;
+  for (int64_t by = (int64_t)blockIdx.y * 32; by < rows; by += (int64_t)gridDim.y * 32) {
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const int64_t r = by + i, c = bx + threadIdx.x;
+      if (r < rows && c < cols) tile[i][threadIdx.x] = in[r * cols + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+      const int64_t c = bx + i, r = by + threadIdx.x;
+      if (c < cols && r < rows && QG_STORE_OK(kSiteUtil, c * rows + r, rows * cols))
+        out[c * rows + r] = tile[threadIdx.x][i];
+    }
+    __syncthreads();
   }
 }
 
@@ -57,7 +61,8 @@ unsigned grid_for(int64_t n) {
 
 cudaError_t launch_transpose(Ctx* ctx, const double* in, int64_t rows, int64_t cols, double* out) {
   if (rows <= 0 || cols <= 0) return cudaSuccess;
-  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)((rows + 31) / 32));
+  const int64_t row_blocks = (rows + 31) / 32;
+  dim3 grid((unsigned)((cols + 31) / 32), (unsigned)(row_blocks < 65535 ? row_blocks : 65535));
   LaunchScope scope(ctx, "transpose");
   transpose_kernel<<<grid, dim3(32, 8), 0, ctx->stream>>>(in, rows, cols, out);
   return cudaGetLastError();
