@@ -216,7 +216,7 @@ struct AoBasisData {
 
 // The host-buffer path's contraction jobs (one per point range), kept on the device while the
 // shape and buffers they were encoded for stay the same.
-constexpr int kMaxHostChunks = 16;
+constexpr int kMaxHostChunks = 32;
 struct HostChunkKey {
   int64_t P = 0, M = 0, kp = 0;
   int chunks = 0;

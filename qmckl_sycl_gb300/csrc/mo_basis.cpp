@@ -213,6 +213,14 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
 // earlier start of the copies gains.
 constexpr int kHostChunks = 6;
 constexpr double kHostChunkRatio = 1.0;
+// Larger point sets use more ranges, of at least this many points each (the medium workload's
+// sixth), so that the first range, whose compute the link waits for, stays short.
+constexpr int64_t kHostChunkPoints = 6827;
+
+static int host_chunk_count(int64_t P) {
+  const int64_t n = (P + kHostChunkPoints - 1) / kHostChunkPoints;
+  return (int)(n < kHostChunks ? kHostChunks : (n > kMaxHostChunks ? kMaxHostChunks : n));
+}
 
 // QMCKL_GB300_HOST_CHUNKS="<ranges>[,<ratio>]" overrides the plan (for measurements).
 static void host_chunk_plan_override(int* chunks, double* ratio) {
@@ -249,7 +257,7 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
     // equal point ranges (QMCKL_GB300_HOST_CHUNKS="<ranges>,<ratio>" overrides the plan); the
     // device-to-host link (~193 GB/s) needs 2.54 ms for the medium workload's 491 MB of mo_vgl,
     // the computation 1.73 ms
-    int chunks = kHostChunks;
+    int chunks = host_chunk_count(ctx->point.num);
     double ratio = kHostChunkRatio;
     host_chunk_plan_override(&chunks, &ratio);
     qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, chunks, ratio);
