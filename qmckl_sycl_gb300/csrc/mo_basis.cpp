@@ -213,13 +213,16 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
 // earlier start of the copies gains.
 constexpr int kHostChunks = 6;
 constexpr double kHostChunkRatio = 1.0;
-// Larger point sets use more ranges, of at least this many points each (the medium workload's
-// sixth), so that the first range, whose compute the link waits for, stays short.
-constexpr int64_t kHostChunkPoints = 6827;
+// Larger point sets use more ranges, of about this many points each, up to kHostChunksMax, so that
+// the first range, whose compute the link waits for, stays short. Measured end to end (ms per
+// step; link time alone 10.2 / 63.6 ms): 163,840 points 11.46 / 10.98 / 11.29 ms with 6 / 12 / 24
+// ranges; 1,024,000 points 74.1 / 69.8 / 74.6 ms with 6 / 16 / 32 ranges.
+constexpr int64_t kHostChunkPoints = 13653;
+constexpr int kHostChunksMax = 16;
 
 static int host_chunk_count(int64_t P) {
   const int64_t n = (P + kHostChunkPoints - 1) / kHostChunkPoints;
-  return (int)(n < kHostChunks ? kHostChunks : (n > kMaxHostChunks ? kMaxHostChunks : n));
+  return (int)(n < kHostChunks ? kHostChunks : (n > kHostChunksMax ? kHostChunksMax : n));
 }
 
 // QMCKL_GB300_HOST_CHUNKS="<ranges>[,<ratio>]" overrides the plan (for measurements).
