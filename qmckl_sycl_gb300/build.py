@@ -5,13 +5,14 @@ and linked into one shared library exporting the C ABI of include/qmckl_gpu.h. H
 is compiled without floating-point contraction so that host-side table arithmetic rounds
 like the reference.
 
-    python -m qmckl_sycl_gb300.build [--force] [--verbose] [--bounds]
+    python -m qmckl_sycl_gb300.build [--force] [--verbose] [--bounds | --sanitize]
 
 --bounds builds the debug variant _lib/libqmckl_gpu_bounds.so instead (objects in _build_bounds/),
 compiled with -DQMCKL_BOUNDS_CHECK: every checked global store of the kernels tests its index
 against the array's extent and records the first violation (qmckl_bounds_check_status_device).
 --sanitize builds _lib/libqmckl_gpu_asan.so (objects in _build_asan/): host code with
-AddressSanitizer and UndefinedBehaviorSanitizer, for the CPU tests of the argument paths.
+AddressSanitizer and UndefinedBehaviorSanitizer, for the tests of the host code (argument paths
+on the CPU, whole evaluations on the GPU); load it with libasan preloaded.
 """
 import os
 import subprocess
@@ -55,11 +56,11 @@ def _headers_mtime():
     return m
 
 
-def _compile(src, verbose, build_dir=BUILD, extra=(), arch=ARCH):
+def _compile(src, verbose, build_dir=BUILD, extra=()):
     obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), _headers_mtime()):
         return obj
-    flags = list(arch) + COMMON + list(extra)
+    flags = ARCH + COMMON + list(extra)
     cmd = [nvcc()] + flags + ["-c", src, "-o", obj]
     if src.endswith(".cpp"):
         cmd = [nvcc(), "-x", "cu"] + flags + ["-c", src, "-o", obj]
@@ -74,8 +75,8 @@ def _compile(src, verbose, build_dir=BUILD, extra=(), arch=ARCH):
     return obj
 
 
-# Host code under AddressSanitizer and UndefinedBehaviorSanitizer, for the CPU tests of the
-# C ABI's argument paths (device code as PTX only: that build never runs a kernel).
+# Host code under AddressSanitizer and UndefinedBehaviorSanitizer (device code as usual), for the
+# tests of the C ABI's host code: argument paths on the CPU, whole evaluations on the GPU.
 SANITIZE = ["-Xcompiler", "-fsanitize=address,-fsanitize=undefined,-fno-sanitize-recover=all,-fno-omit-frame-pointer,-g"]
 
 
@@ -83,7 +84,6 @@ def build(force=False, verbose=False, jobs=None, bounds=False, sanitize=False):
     build_dir = BUILD + ("_bounds" if bounds else "_asan" if sanitize else "")
     lib = BOUNDS_LIB if bounds else (ASAN_LIB if sanitize else LIB)
     extra = ["-DQMCKL_BOUNDS_CHECK"] if bounds else (SANITIZE if sanitize else [])
-    arch = ["-gencode", "arch=compute_103a,code=compute_103a"] if sanitize else ARCH
     os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = sources()
@@ -92,12 +92,12 @@ def build(force=False, verbose=False, jobs=None, bounds=False, sanitize=False):
             if f.endswith(".o"):
                 os.remove(os.path.join(build_dir, f))
     with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose, build_dir, extra, arch), srcs))
+        objs = list(ex.map(lambda s: _compile(s, verbose, build_dir, extra), srcs))
     if (not force and os.path.exists(lib)
             and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs)):
         return lib
     tmp = lib + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + arch + (SANITIZE if sanitize else []) + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + (SANITIZE if sanitize else []) + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))
