@@ -545,6 +545,36 @@ int32_t qmckl_bounds_check_status_device(int32_t reset, int64_t* site, int64_t* 
  * build, -2 on a CUDA error. */
 int32_t qmckl_bounds_check_selftest_device(int64_t index, int64_t extent);
 
+/* ---- TREXIO reader (reference: src/qmckl_trexio.cpp, include/qmckl_trexio.hpp) ----
+ * Fills a context from a TREXIO file through the setters above. libtrexio is bound at run time
+ * (dlopen of $QMCKL_TREXIO_LIBRARY, else libtrexio.so, else libtrexio.so.2), so this library links
+ * and loads without it; where it cannot be loaded these calls return QMCKL_FAILURE_DEVICE (open:
+ * NULL) with the loader's message. trexio_t is libtrexio's opaque file handle. The shells of one
+ * nucleus and the primitives of one shell must be contiguous in the file (else QMCKL_FAILURE_DEVICE,
+ * "Irrelevant data in TREXIO file"; the reference accepts such files and mis-assigns them). */
+typedef struct trexio_s trexio_t;
+/* src/qmckl_trexio.cpp:937-958: opens file_name read-only with the text back end, else HDF5; NULL
+ * and *rc = QMCKL_FAILURE_DEVICE when neither opens. Close the handle with libtrexio's trexio_close. */
+trexio_t* qmckl_trexio_open_X_device(char* file_name, qmckl_exit_code_device* rc);
+/* src/qmckl_trexio.cpp:7-41: electron.up_num and dn_num -> qmckl_set_electron_num_device */
+qmckl_exit_code_device qmckl_trexio_read_electron_X_device(qmckl_context_device context, trexio_t* file);
+/* src/qmckl_trexio.cpp:43-141: nucleus.num, charge and coord ([nucleus][3], set with 'N') */
+qmckl_exit_code_device qmckl_trexio_read_nucleus_X_device(qmckl_context_device context, trexio_t* file);
+/* src/qmckl_trexio.cpp:143-866: the basis (Gaussian only: "Invalid basis type" otherwise) and
+ * ao.num/normalization; the nucleus of each shell and the shell of each primitive become each
+ * nucleus's first shell and shell count and each shell's first primitive and primitive count.
+ * Needs the nucleus number set. */
+qmckl_exit_code_device qmckl_trexio_read_ao_X_device(qmckl_context_device context, trexio_t* file);
+/* src/qmckl_trexio.cpp:868-935: mo.num and mo.coefficient ([mo][ao], read size-checked as
+ * ao_num * mo_num values). Needs ao_num set. */
+qmckl_exit_code_device qmckl_trexio_read_mo_X_device(qmckl_context_device context, trexio_t* file);
+/* src/qmckl_trexio.cpp:960-1021: all four, in that order, from the file named by the first
+ * size_max characters of file_name. A file that opens with neither back end:
+ * QMCKL_INVALID_ARG_2_DEVICE; a failing group: QMCKL_FAILURE_DEVICE ("Error reading electron",
+ * "... nucleus", "... AOs", "... MOs"). NULL context: QMCKL_INVALID_CONTEXT_DEVICE (the reference
+ * returns 0). */
+qmckl_exit_code_device qmckl_trexio_read_device(qmckl_context_device context, char* file_name, int64_t size_max);
+
 /* Library build information: "sm_103a" plus the git-independent build flags. */
 const char* qmckl_gb300_build_info(void);
 

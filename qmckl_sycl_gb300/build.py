@@ -97,7 +97,7 @@ def build(force=False, verbose=False, jobs=None, bounds=False, sanitize=False):
             and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs)):
         return lib
     tmp = lib + ".tmp%d" % os.getpid()
-    cmd = [nvcc()] + ARCH + (SANITIZE if sanitize else []) + ["-shared", "-o", tmp] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + (SANITIZE if sanitize else []) + ["-shared", "-o", tmp] + objs + ["-lcudart", "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

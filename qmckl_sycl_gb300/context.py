@@ -7,6 +7,7 @@ exit code on failure. `load_system` calls the setters in the order of the refere
 tests (tests/test_qmckl_ao.cpp:122-176, tests/test_qmckl_mo.cpp:80-275).
 """
 import ctypes
+import os
 
 import numpy as np
 
@@ -158,6 +159,12 @@ class Context:
         self.call("set_mo_basis_mo_num", s.mo_num)
         d = self.upload(s.mo_coef)
         self.call("set_mo_basis_coefficient", d.ptr)
+
+    def read_trexio(self, path):
+        """Electrons, nuclei, basis, AOs and MOs from a TREXIO file (qmckl_trexio_read_device;
+        libtrexio is loaded at run time, see include/qmckl_gpu.h)."""
+        name = os.fsencode(path)
+        self.call("trexio_read", name, len(name))
 
     def set_point(self, coord, transp="N", host=False):
         """coord is [P][3] for 'N' or [3][P] for 'T'. With host=True the host array is

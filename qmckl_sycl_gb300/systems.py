@@ -134,6 +134,20 @@ SPD_WEIGHTS = (0.55, 0.40, 0.05)
 SPDF_WEIGHTS = (0.62, 0.30, 0.06, 0.02)
 
 
+def with_empty_nucleus(s, at, xyz=(0.7, -1.1, 0.3), charge=1.0):
+    """s with one more centre, inserted at position `at`, that owns no shell (a bare charge): its
+    nucleus_index entry is 0 and its shell count 0. Its AO and MO values are those of s."""
+    d = dict(s.__dict__)
+    ins = lambda a, v: np.insert(np.asarray(a), at, v)
+    d["nucl_num"] = s.nucl_num + 1
+    d["charge"] = ins(s.charge, charge)
+    d["nucl_coord"] = np.ascontiguousarray(np.insert(s.nucl_coord, at, list(xyz), axis=1))
+    d["nucleus_index"] = ins(s.nucleus_index, 0).astype(np.int64)
+    d["nucleus_shell_num"] = ins(s.nucleus_shell_num, 0).astype(np.int64)
+    d["name"] = "%s+empty@%d" % (s.name, at)
+    return System(**d)
+
+
 def config_small(seed=0, point_num=50):
     return make_system(seed, 6, 8, 6.0, 60, SPD_WEIGHTS, 5, (0.05, 50.0), 40, point_num, 1.5, name="small")
 

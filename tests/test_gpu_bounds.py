@@ -3,7 +3,7 @@ _lib/libqmckl_gpu_bounds.so). Every checked store tests its element index agains
 of the array it writes; an out-of-range store is skipped and the first one recorded, with no
 trap or assert. A child process loads that build (QMCKL_GB300_BOUNDS_CHECK=1) and runs the small
 cases of every path (FP64 and split-BF16 AO/MO vgl and values, shell radials, ragged point
-counts, the host-buffer chunked path, distances, the adjoint, a batch, the allocation-free
+counts, centres without shells, the host-buffer chunked path, distances, the adjoint, a batch, the allocation-free
 contraction); no store may have been out of range, and the results must still match the oracle.
 The recording itself is checked first with the self-test kernel (an index past its extent,
 nothing stored)."""
@@ -25,7 +25,7 @@ sys.path.insert(0, sys.argv[1] + "/tests")
 from conftest import normwise_rel_err
 from oracle import oracle
 from qmckl_sycl_gb300 import capi, Batch, Context, config_adjoint, config_batched, config_medium, config_small
-from qmckl_sycl_gb300.systems import System
+from qmckl_sycl_gb300.systems import System, with_empty_nucleus
 
 L = capi.lib()
 assert b"bounds-check" in L.qmckl_gb300_build_info(), L.qmckl_gb300_build_info()
@@ -44,6 +44,7 @@ with Context(0) as ctx:  # makes device 0 current
 
 chbrclf = System.from_npz(sys.argv[1] + "/tests/golden/chbrclf.npz")
 cases = [chbrclf, config_small(0), config_adjoint(0)] + [config_small(1, point_num=n) for n in (1, 33, 97)]
+cases += [with_empty_nucleus(chbrclf, 0), with_empty_nucleus(config_small(2), 6)]  # centres without shells
 for s in cases:
     ref = oracle.forward(s)
     for mode, tol in ((0, 1e-12), (1, 1e-6)):

@@ -10,6 +10,7 @@ import pytest
 from conftest import normwise_rel_err
 from oracle import oracle
 from qmckl_sycl_gb300 import Context, QmcklError, config_adjoint, config_medium, config_small
+from qmckl_sycl_gb300.systems import with_empty_nucleus
 
 pytestmark = pytest.mark.gpu
 
@@ -35,10 +36,11 @@ def check(out, ref, keys=("ao_vgl", "ao_value", "mo_vgl", "mo_value")):
             assert np.array_equal(out[k] == 0.0, ref[k] == 0.0), "%s screening pattern differs" % k
 
 
-@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium_sub"])
+@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium_sub", "small_empty_nucleus"])
 def test_forward_matches_oracle(name, chbrclf):
     s = {"chbrclf": lambda: chbrclf, "small": lambda: config_small(0), "adjoint": lambda: config_adjoint(0),
-         "medium_sub": lambda: config_medium(0, walkers=16, electrons=160)}[name]()
+         "medium_sub": lambda: config_medium(0, walkers=16, electrons=160),
+         "small_empty_nucleus": lambda: with_empty_nucleus(config_small(0), 3)}[name]()
     ref = oracle.forward(s)
     check(run_all(s), ref)
 

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from qmckl_sycl_gb300.systems import config_adjoint, config_medium, config_small
+from qmckl_sycl_gb300.systems import config_adjoint, config_medium, config_small, with_empty_nucleus
 
 
 def test_oracle_matches_golden_mo_vgl(chbrclf, golden):
@@ -34,17 +34,28 @@ def test_oracle_mo_value_consistent_with_mo_vgl(chbrclf):
     assert np.abs(out["mo_value"] - out["mo_vgl"][:, 0, :]).max() <= 1e-12
 
 
-@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium64"])
+@pytest.mark.parametrize("name", ["chbrclf", "small", "adjoint", "medium64", "chbrclf_empty_nucleus"])
 def test_oracle_bitwise_equal_to_reference(name, chbrclf):
     if oracle.reference_lib() is None:
         pytest.skip("reference library not built on this machine (needs the reference checkout)")
     s = {"chbrclf": lambda: chbrclf, "small": lambda: config_small(0), "adjoint": lambda: config_adjoint(0),
-         "medium64": lambda: config_medium(0, walkers=1, electrons=64)}[name]()
+         "medium64": lambda: config_medium(0, walkers=1, electrons=64),
+         "chbrclf_empty_nucleus": lambda: with_empty_nucleus(chbrclf, 2)}[name]()
     want = ("ao_vgl", "ao_value", "mo_vgl", "mo_value")
     r = oracle.reference_forward(s, want=want)
     o = oracle.forward(s, want=want)
     for k in want:
         assert np.array_equal(r[k], o[k]), k
+
+
+@pytest.mark.parametrize("at", [0, 2, 5])
+def test_oracle_centre_without_shells(chbrclf, at):
+    # a centre that owns no shell (nucleus_shell_num 0) changes no AO or MO value
+    want = ("ao_vgl", "ao_value", "mo_vgl", "mo_value")
+    a = oracle.forward(chbrclf, want=want)
+    b = oracle.forward(with_empty_nucleus(chbrclf, at), want=want)
+    for k in want:
+        assert np.array_equal(a[k], b[k]), k
 
 
 def test_oracle_nan_coordinates_equal_to_reference():

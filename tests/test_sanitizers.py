@@ -5,8 +5,9 @@ not available for the device side, whose stores the bounds-checked build covers 
   molecule, the small and adjoint systems, NaN coordinates, the per-nucleus tables, distances and
   the FP64 reference gradient, and must give the normal build's bits;
 - the C ABI's host-side argument paths (tests/test_capi.py: NULL and invalid contexts, bad sizes,
-  setter order, masks, registries, test hooks) run against the library whose host code is built
-  with the same sanitizers.
+  setter order, masks, registries, test hooks; tests/test_trexio.py: the TREXIO reader's binding,
+  file opening and table conversion) run against the library whose host code is built with the
+  same sanitizers.
 
 Each runs in a child process with libasan preloaded; any report aborts the child."""
 import os
@@ -87,6 +88,7 @@ def test_c_abi_argument_paths_under_address_and_undefined_behaviour_sanitizers()
     build.build(sanitize=True)
     build.build()
     r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "-p", "no:cacheprovider",
-                        os.path.join(ROOT, "tests", "test_capi.py")], capture_output=True, text=True, timeout=900,
+                        os.path.join(ROOT, "tests", "test_capi.py"), os.path.join(ROOT, "tests", "test_trexio.py")],
+                       capture_output=True, text=True, timeout=900,
                        cwd=ROOT, env=_asan_env(QMCKL_GB300_SANITIZE="1"))
     assert r.returncode == 0 and " passed" in r.stdout, r.stdout[-4000:] + r.stderr[-4000:]
