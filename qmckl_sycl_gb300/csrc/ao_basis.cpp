@@ -182,12 +182,30 @@ void split_chunks(const std::vector<NucleusEntry>& nuc, const std::vector<double
       if (k < parts - 1 && acc >= target) break;
     }
     if (end == begin) end = begin + 1;
-    out.push_back(NucleusChunk{begin, end, nuc[begin].ao_begin, nuc[end - 1].ao_end});
+    out.push_back(NucleusChunk{begin, end, nuc[begin].ao_begin, nuc[end - 1].ao_end, nuc[begin].shell_begin,
+                               nuc[end - 1].shell_end});
     begin = end;
   }
   if (begin < n) {  // leftovers go to the last chunk
     out.back().nucl_end = n;
     out.back().ao_end = nuc[n - 1].ao_end;
+    out.back().shell_hi = nuc[n - 1].shell_end;
+  }
+}
+
+// Pieces: each nucleus's shells in consecutive ranges of cost about `target` (at least one shell
+// each; nuclei without shells have none), appended to out.
+void split_pieces(const std::vector<NucleusEntry>& nuc, const std::vector<ShellEntry>& shells,
+                  const std::vector<double>& shell_cost, double target, std::vector<NucleusChunk>& out) {
+  for (int n = 0; n < (int)nuc.size(); ++n) {
+    int s = nuc[n].shell_begin;
+    while (s < nuc[n].shell_end) {
+      const int lo = s;
+      double acc = shell_cost[s++];
+      while (s < nuc[n].shell_end && acc + shell_cost[s] <= target) acc += shell_cost[s++];
+      const int ao_hi = s < nuc[n].shell_end ? shells[s].ao_begin : nuc[n].ao_end;
+      out.push_back(NucleusChunk{n, n + 1, shells[lo].ao_begin, ao_hi, lo, s});
+    }
   }
 }
 
@@ -228,7 +246,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   t.h_shell_nucl.clear();
   t.level_offsets.clear();
   t.level_sizes.clear();
-  std::vector<double> cost;
+  std::vector<double> cost, shell_cost;
   int ao_counter = 0, lmax = 0;
   for (int64_t n = 0; n < N; ++n) {
     NucleusEntry e{};
@@ -266,6 +284,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
       ao_counter += ncart(l);
       e.lmax = std::max(e.lmax, l);
       w += (double)spn[s] + 0.5 * ncart(l);
+      shell_cost.push_back((double)spn[s] + 0.5 * ncart(l));
       t.h_shells.push_back(se);
       t.h_shell_orig.push_back((int32_t)s);
       t.h_shell_nucl.push_back((int32_t)n);
@@ -287,6 +306,13 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
     split_chunks(t.h_nuclei, cost, p, t.h_chunks);
     t.level_sizes.push_back((int32_t)(t.h_chunks.size() - before));
     if (p >= N) break;
+  }
+  {
+    double total = 0.0;
+    for (double c : cost) total += c - 1.0;
+    t.piece_offset = (int32_t)t.h_chunks.size();
+    split_pieces(t.h_nuclei, t.h_shells, shell_cost, total / (4.0 * (double)N), t.h_chunks);
+    t.piece_num = (int32_t)t.h_chunks.size() - t.piece_offset;
   }
   t.h_ao_factor = aof;
   // 2^(j/32) to ~64 bits: hi = nearest double, lo = remainder (long double on the host)

@@ -52,12 +52,12 @@ constexpr int kWarps = 4;          // warps per CTA (each runs its own task)
 #endif
 // Tasks per resident warp the nucleus-chunk level is chosen for (finer chunks give more tasks).
 constexpr int kTasksPerWarp = QMCKL_AO_TASKS_PER_WARP;
-#ifndef QMCKL_AO_FINE_TAIL
-#define QMCKL_AO_FINE_TAIL 1
+#ifndef QMCKL_AO_TAIL_SEGMENTS
+#define QMCKL_AO_TAIL_SEGMENTS 8
 #endif
-// The last tasks of a launch are split this many levels finer (0: not at all). Measured on the
-// medium workload's planes kernel: 0.997 / 0.991 / 0.993 / 0.991 ms for 0 / 1 / 2 / 3 levels.
-constexpr int kFineTailLevels = QMCKL_AO_FINE_TAIL;
+// Segments of a launch's schedule (1: every task at the chosen level; more: the last point
+// groups at finer levels, down to pieces of nuclei).
+constexpr int kTailSegments = QMCKL_AO_TAIL_SEGMENTS;
 using namespace dev;
 
 enum class Out { Vgl, Value, Planes };
@@ -514,17 +514,24 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
                                         const double* __restrict__ thi, const double* __restrict__ tlo,
                                         const double* __restrict__ fine, double* __restrict__ ebuf, int lane) {
   constexpr int NC = ncomp<O>();
-  int64_t group;
-  const NucleusChunk* chunk;
-  if (task < a.tail_task) {
-    group = task / a.chunk_num;
-    chunk = a.chunks + (task - group * a.chunk_num);
-  } else {  // the finer tail
-    const int64_t t = task - a.tail_task;
-    const int64_t g = t / a.tail_chunk_num;
-    group = a.tail_group + g;
-    chunk = a.tail_chunks + (t - g * a.tail_chunk_num);
+  // the task's segment (the last one starting at or before it), selected with constant indices
+  // so that the kernel-parameter arrays are read in place
+  int64_t t0 = a.seg_task[0], g0 = a.seg_group[0];
+  const NucleusChunk* c0 = a.seg_chunks[0];
+  int cn = a.seg_chunk_num[0];
+#pragma unroll
+  for (int k = 1; k < FusedArgs::kMaxSegments; ++k) {
+    if (k < a.nseg && task >= a.seg_task[k]) {
+      t0 = a.seg_task[k];
+      g0 = a.seg_group[k];
+      c0 = a.seg_chunks[k];
+      cn = a.seg_chunk_num[k];
+    }
   }
+  const int64_t t = task - t0;
+  const int64_t g = t / cn;
+  const int64_t group = g0 + g;
+  const NucleusChunk* chunk = c0 + (t - g * cn);
   const int64_t p0 = group * 32;
   const int64_t remaining = a.point_num - p0;
   const int nvalid = remaining < 32 ? (int)remaining : 32;
@@ -538,6 +545,8 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
 
   for (int n = cj.nucl_begin; n < cj.nucl_end; ++n) {
     const NucleusEntry& N = a.nuclei[n];
+    // the nucleus's shells, or the chunk's part of them (a piece)
+    const int s_begin = max(N.shell_begin, cj.shell_lo), s_end = min(N.shell_end, cj.shell_hi);
     const double x = ex - N.x, y = ey - N.y, z = ez - N.z;
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
     const uint64_t r2b = bits_of(r2);
@@ -552,7 +561,9 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     const bool scr = r2b - N.screen_bits - 1ull < 0x7FF0000000000000ull - N.screen_bits;
     const bool nan_warp = __any_sync(kFull, nanr);  // warp-uniform: the NaN fix-up below costs a branch
     if (__all_sync(kFull, scr)) {
-      w.emit_zeros(N.ao_end - N.ao_begin);
+      const int ao_lo = s_begin == N.shell_begin ? N.ao_begin : a.shells[s_begin].ao_begin;
+      const int ao_hi = s_end == N.shell_end ? N.ao_end : a.shells[s_end].ao_begin;
+      w.emit_zeros(ao_hi - ao_lo);
       continue;
     }
     float xf = 0.f, yf = 0.f, zf = 0.f, r2f = 0.f;
@@ -584,7 +595,7 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
         }
       }
     }
-    for (int si = N.shell_begin; si < N.shell_end; ++si) {
+    for (int si = s_begin; si < s_end; ++si) {
       const ShellEntry S = a.shells[si];
       double t0 = 0.0, g = 0.0, h = 0.0;
       bool folded = false;
@@ -898,14 +909,13 @@ __global__ void cell_scatter_kernel(const int32_t* __restrict__ keys, int64_t P,
   if (QG_STORE_OK(kSitePointPerm, pos, P)) perm[pos] = (int32_t)p;
 }
 
-// Picks the first nucleus-chunk level with at least `target` warp tasks.
+// Picks the first nucleus-chunk level with at least `target` warp tasks; when none has that
+// many, the pieces (level index ao_level_count(t)) if there are more of them.
 int pick_level(const AoTables& t, int64_t groups, int64_t target) {
-  int best = 0;
-  for (int lv = 0; lv < (int)t.level_offsets.size(); ++lv) {
-    best = lv;
-    if (groups * (int64_t)t.level_sizes[lv] >= target) break;
-  }
-  return best;
+  const int levels = (int)t.level_offsets.size();
+  for (int lv = 0; lv < levels; ++lv)
+    if (groups * (int64_t)t.level_sizes[lv] >= target) return lv;
+  return t.piece_num > t.level_sizes[levels - 1] ? levels : levels - 1;
 }
 
 
@@ -937,9 +947,14 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
   // workload, 16 % idle FP64 issue)
   const int level = pick_level(t, groups, kTasksPerWarp * resident_warps);
   FusedArgs a = make_fused_args(t, level, coord, perm, point_num, out, planes, row_len);
-  // the last tasks at a finer level: a warp's last task is short, so the launch ends with every
-  // warp busy nearly to the end (a task at the coarse level takes ~1/3 of the launch)
-  if (kFineTailLevels > 0) set_fine_tail(a, t, level + kFineTailLevels, resident_warps);
+  // the last tasks at ever finer levels down to the pieces: a warp's last task is short, so the
+  // launch ends with every warp busy nearly to the end (a task at the coarse level takes ~1/3
+  // of the launch, and a lone warp runs a nucleus's FP64 work on one sub-partition's FP64 unit).
+  // Measured on the medium workload's planes (40,960 points): 0.982 ms against 1.005 ms for one
+  // segment; with about 4 or 16 times as many tail tasks 1.010 / 1.062 ms, and with 4, 8 or 32
+  // tasks per warp at the coarse level 1.05 / 1.09 / 1.36 ms (finer tasks cost more than they
+  // balance: every task takes a global counter and reloads its points).
+  plan_segments(a, t, level, resident_warps, kTailSegments);
   if (coord_ld >= 0) a.coord_ld = coord_ld;
   a.ent = B ? t.ent : nullptr;
   a.ent_cap = B ? t.ent_cap : 0;
@@ -1029,6 +1044,37 @@ __global__ void batch_scatter_kernel(const OrderDesc* __restrict__ desc, const i
   if (QG_STORE_OK(kSitePointPerm, pos, d.point_num)) d.perm[pos] = (int32_t)p;
 }
 
+// The range of point p among nr consecutive ranges: the last r with bounds[r] <= p.
+__device__ __forceinline__ int range_of(const int64_t* __restrict__ bounds, int nr, int64_t p) {
+  int lo = 0, hi = nr - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bounds[mid] <= p) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void range_key_kernel(const double* __restrict__ coord, int64_t P, double ox, double oy, double oz,
+                                 double inv_cell, const int64_t* __restrict__ bounds, int nr,
+                                 int32_t* __restrict__ keys, int32_t* __restrict__ counts) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const double origin[3] = {ox, oy, oz};
+  const int key = morton_key(coord[p], coord[P + p], coord[2 * P + p], origin, inv_cell);
+  keys[p] = key;
+  atomicAdd(&counts[(int64_t)range_of(bounds, nr, p) * kOrderCells + key], 1);
+}
+
+__global__ void range_scatter_kernel(const int32_t* __restrict__ keys, int64_t P, const int64_t* __restrict__ bounds,
+                                     int nr, int32_t* __restrict__ offsets, int32_t* __restrict__ perm) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  const int r = range_of(bounds, nr, p);
+  const int64_t at = bounds[r] + atomicAdd(&offsets[(int64_t)r * kOrderCells + keys[p]], 1);
+  if (QG_STORE_OK(kSitePointPerm, at, P)) perm[at] = (int32_t)(p - bounds[r]);
+}
+
 }  // namespace
 
 int ao_level_count(const AoTables& t) { return (int)t.level_offsets.size(); }
@@ -1040,14 +1086,16 @@ bool ao_shared_exponentials(const AoTables& t, bool planes) {
 
 FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
                           double* out, void* planes, int64_t row_len) {
-  const int lv = level < 0 ? 0 : (level >= (int)t.level_offsets.size() ? (int)t.level_offsets.size() - 1 : level);
+  const int levels = (int)t.level_offsets.size();
+  const bool pieces = level >= levels && t.piece_num > 0;
+  const int lv = level < 0 ? 0 : (level >= levels ? levels - 1 : level);
   FusedArgs a;
   a.nuclei = t.nuclei;
   a.shells = t.shells;
   a.prims = t.prims;
   a.aof = t.ao_factor;
-  a.chunk_num = t.level_sizes[lv];
-  a.chunks = t.chunks + t.level_offsets[lv];
+  a.chunk_num = pieces ? t.piece_num : t.level_sizes[lv];
+  a.chunks = t.chunks + (pieces ? t.piece_offset : t.level_offsets[lv]);
   a.exp_table = t.exp_table;
   a.fold = t.fold;
   const bool share = ao_shared_exponentials(t, planes != nullptr);
@@ -1063,26 +1111,52 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.plane_pp = (point_num + 31) / 32 * 32;
   a.coord_ld = point_num;
   a.task_num = ((point_num + 31) / 32) * a.chunk_num;
-  a.tail_chunks = a.chunks;
-  a.tail_chunk_num = a.chunk_num;
-  a.tail_group = (point_num + 31) / 32;
-  a.tail_task = a.task_num;
+  a.nseg = 1;
+  a.seg_task[0] = 0;
+  a.seg_task[1] = a.task_num;
+  a.seg_group[0] = 0;
+  a.seg_chunks[0] = a.chunks;
+  a.seg_chunk_num[0] = a.chunk_num;
   return a;
 }
 
-void set_fine_tail(FusedArgs& a, const AoTables& t, int fine, int64_t tail_tasks) {
-  if (fine <= 0 || fine >= (int)t.level_offsets.size()) return;
-  const int n = t.level_sizes[fine];
-  if (n <= a.chunk_num) return;
+void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_tasks, int max_segments) {
   const int64_t groups = (a.point_num + 31) / 32;
-  int64_t tg = (tail_tasks + n - 1) / n;
-  if (tg > groups / 2) tg = groups / 2;
-  if (tg <= 0) return;
-  a.tail_group = groups - tg;
-  a.tail_task = a.tail_group * a.chunk_num;
-  a.tail_chunks = t.chunks + t.level_offsets[fine];
-  a.tail_chunk_num = n;
-  a.task_num = a.tail_task + tg * n;
+  if (max_segments > FusedArgs::kMaxSegments) max_segments = FusedArgs::kMaxSegments;
+  // finer partitions from the finest up: the pieces, then the levels finer than a's
+  struct Part {
+    const NucleusChunk* chunks;
+    int num;
+  };
+  std::vector<Part> finer;
+  if (t.piece_num > a.chunk_num) finer.push_back(Part{t.chunks + t.piece_offset, t.piece_num});
+  for (int lv = (int)t.level_offsets.size() - 1; lv > level; --lv)
+    if (t.level_sizes[lv] > a.chunk_num && (finer.empty() || t.level_sizes[lv] < finer.back().num))
+      finer.push_back(Part{t.chunks + t.level_offsets[lv], t.level_sizes[lv]});
+  // groups of each finer segment (about tail_tasks tasks), finest first, at most half of all
+  std::vector<int64_t> take;
+  int64_t used = 0;
+  for (const Part& p : finer) {
+    if ((int)take.size() + 1 >= max_segments) break;
+    int64_t g = (tail_tasks + p.num - 1) / p.num;
+    if (used + g > groups / 2) g = groups / 2 - used;
+    if (g <= 0) break;
+    take.push_back(g);
+    used += g;
+  }
+  a.nseg = 1;
+  int64_t group = groups - used, task = group * a.chunk_num;
+  for (int k = (int)take.size() - 1; k >= 0; --k) {  // coarse to fine
+    const int i = a.nseg++;
+    a.seg_task[i] = task;
+    a.seg_group[i] = group;
+    a.seg_chunks[i] = finer[k].chunks;
+    a.seg_chunk_num[i] = finer[k].num;
+    group += take[k];
+    task += take[k] * finer[k].num;
+  }
+  a.seg_task[a.nseg] = task;
+  a.task_num = task;
 }
 
 template <Out O, bool G, bool B>
@@ -1163,6 +1237,26 @@ cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord,
   }
   LaunchScope scope(ctx, "point_order_scatter");
   cell_scatter_kernel<<<blocks, 256, 0, ctx->stream>>>(keys, point_num, counts, perm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_point_order_ranges(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num,
+                                      const int64_t* bounds, int nr, int32_t* keys, int32_t* counts, int32_t* perm) {
+  if (point_num <= 0 || nr <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(counts, 0, sizeof(int32_t) * kOrderCells * (size_t)nr, ctx->stream);
+  if (e != cudaSuccess) return e;
+  const unsigned blocks = (unsigned)((point_num + 255) / 256);
+  {
+    LaunchScope scope(ctx, "point_order_keys");
+    range_key_kernel<<<blocks, 256, 0, ctx->stream>>>(coord, point_num, t.grid_origin[0], t.grid_origin[1],
+                                                      t.grid_origin[2], t.grid_inv_cell, bounds, nr, keys, counts);
+  }
+  {
+    LaunchScope scope(ctx, "point_order_scan");
+    cell_scan_kernel<<<nr, 1024, 0, ctx->stream>>>(counts);
+  }
+  LaunchScope scope(ctx, "point_order_scatter");
+  range_scatter_kernel<<<blocks, 256, 0, ctx->stream>>>(keys, point_num, bounds, nr, counts, perm);
   return cudaGetLastError();
 }
 

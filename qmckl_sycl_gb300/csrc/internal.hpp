@@ -70,6 +70,7 @@ struct PrimEntry {         // 48 bytes
 struct NucleusChunk {
   int32_t nucl_begin, nucl_end;
   int32_t ao_begin, ao_end;
+  int32_t shell_lo, shell_hi;  // packed shells evaluated: all of the nuclei's, or part of one nucleus's
 };
 
 // 2^(j/32), j = 0..31, as hi + lo doubles (hi = the double nearest to the value): the table of
@@ -111,6 +112,10 @@ struct AoTables {
   // Level v splits the nuclei into level_sizes[v] chunks of balanced cost, stored at
   // chunks + level_offsets[v]; the launch picks the level that fills the GPU.
   std::vector<int32_t> level_offsets, level_sizes;
+  // Pieces: every nucleus's shells cut into consecutive ranges of about a quarter of a nucleus's
+  // average cost, one chunk each, at chunks + piece_offset (after the levels; the finest tasks of
+  // the forward AO kernel's last segment).
+  int32_t piece_offset = 0, piece_num = 0;
   ExpTable* exp_table = nullptr;    // device copy of the exponential's table
   // [prim_num] packed, or null when some exponent or coefficient is outside the folded
   // evaluation's range (then the split-BF16 form evaluates its radials like the FP64 form)
@@ -379,6 +384,11 @@ constexpr int kOrderCells = 32 * 32 * 32;
 // sort of their Morton cell keys); keys [P] and counts [kOrderCells] are scratch.
 cudaError_t launch_point_order(Ctx* ctx, const AoTables& t, const double* coord, int64_t coord_ld, int64_t point_num,
                                int32_t* keys, int32_t* counts, int32_t* perm);
+// The same for nr consecutive ranges of a point set of point_num points (coordinates [3][point_num]):
+// range r covers points bounds[r] .. bounds[r + 1] - 1 (bounds on the device) and is ordered on its
+// own; perm[bounds[r] + i] holds range-local point indices. counts holds nr * kOrderCells counters.
+cudaError_t launch_point_order_ranges(Ctx* ctx, const AoTables& t, const double* coord, int64_t point_num,
+                                      const int64_t* bounds, int nr, int32_t* keys, int32_t* counts, int32_t* perm);
 // Fused AO kernels; perm (may be null) is the processing order of the points.
 cudaError_t launch_ao_vgl(Ctx* ctx, const AoTables& t, const double* coord, const int32_t* perm, int64_t point_num,
                           double* ao_vgl);
@@ -431,13 +441,16 @@ struct FusedArgs {
   int64_t coord_ld;         // row stride of coord (point_num, or more for a slice of a larger set)
   int64_t task_num;
   int chunk_num;
-  // Finer tasks at the end: point groups from tail_group on are split at a finer nucleus-chunk
-  // level (tail_chunks, tail_chunk_num chunks), numbered from tail_task = tail_group * chunk_num,
-  // so that the last tasks the warps take are short. tail_task == task_num: no such groups.
-  const NucleusChunk* tail_chunks;
-  int64_t tail_group;
-  int64_t tail_task;
-  int tail_chunk_num;
+  // The point groups in nseg consecutive segments, coarse to fine: segment i covers groups from
+  // seg_group[i] on, split at its own chunk level (seg_chunks, seg_chunk_num[i] chunks), and its
+  // tasks are numbered from seg_task[i] (seg_task[nseg] = task_num). The finer segments at the
+  // end make the last tasks the warps take short.
+  static constexpr int kMaxSegments = 8;
+  int nseg;
+  int64_t seg_task[kMaxSegments + 1];
+  int64_t seg_group[kMaxSegments];
+  const NucleusChunk* seg_chunks[kMaxSegments];
+  int seg_chunk_num[kMaxSegments];
 };
 // Number of nucleus-chunk levels of the tables (level v has about 2^v chunks).
 int ao_level_count(const AoTables& t);
@@ -447,9 +460,10 @@ int ao_level_count(const AoTables& t);
 bool ao_shared_exponentials(const AoTables& t, bool planes);
 FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
                           double* out, void* planes, int64_t row_len);
-// Splits the last point groups of a at the finer nucleus-chunk level `fine` (about tail_tasks
-// tasks, at most half of the groups; nothing when that level is not finer than a's).
-void set_fine_tail(FusedArgs& a, const AoTables& t, int fine, int64_t tail_tasks);
+// Ends a's schedule with finer segments: from the pieces up through the levels finer than a's,
+// each holding about tail_tasks tasks, at most max_segments segments in all and at most half of
+// the point groups in the finer ones.
+void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_tasks, int max_segments);
 // Persistent AO kernel over the tasks of nmol molecules: mols[m]'s tasks are numbered from
 // task_begin[m] (non-decreasing, task_begin[nmol] = total); warps take tasks from *counter
 // (zeroed before the launch). planes selects the BF16-plane output; high_l must be set when

@@ -205,20 +205,21 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
   return QMCKL_SUCCESS_DEVICE;
 }
 
-// Point ranges of the host-buffer path and their size ratio (1: equal ranges). Measured end to
-// end on the medium workload (set_point from and mo_vgl into page-locked host memory, ms per
-// step): 6 equal ranges 3.01, 5 3.13, 7 3.02, 8 2.98, 10 3.32; ranges growing by 1.15 / 1.45 per
-// range (a small first range starts the link early) 3.06 / 3.38, shrinking by 0.85 / 0.7 3.16 /
-// 3.32. The small ranges' kernels run far below the full-size rates, which costs more than the
-// earlier start of the copies gains.
+// Point ranges of the host-buffer path and their size ratio (1: equal ranges). All ranges are
+// put in processing order by one pass before the first range computes, and small ranges take
+// the AO kernel's finest tasks (pieces of nuclei), so the per-range cost is small and many ranges
+// pay: the first range, whose compute the link waits for, stays short. Measured end to end
+// (set_point from and mo_vgl into page-locked host memory, ms per step; the link alone needs
+// 2.55 / 10.2 / 63.6 ms): 40,960 points 3.14 / 3.01 / 2.94 / 2.91 / 2.87 / 2.87 / 3.01 ms with
+// 4 / 6 / 8 / 10 / 12 / 14 / 16 ranges; 163,840 points 11.19 / 10.98 / 10.84 / 10.73 / 10.67 ms
+// with 8 / 12 / 16 / 24 / 32; 1,024,000 points 66.6 / 65.8 / 65.4 ms with 16 / 24 / 32. Ranges of
+// unequal size measured slower (a small first range runs its kernels far below the full-size
+// rates).
 constexpr int kHostChunks = 6;
 constexpr double kHostChunkRatio = 1.0;
-// Larger point sets use more ranges, of about this many points each, up to kHostChunksMax, so that
-// the first range, whose compute the link waits for, stays short. Measured end to end (ms per
-// step; link time alone 10.2 / 63.6 ms): 163,840 points 11.46 / 10.98 / 11.29 ms with 6 / 12 / 24
-// ranges; 1,024,000 points 74.1 / 69.8 / 74.6 ms with 6 / 16 / 32 ranges.
-constexpr int64_t kHostChunkPoints = 13653;
-constexpr int kHostChunksMax = 16;
+// Ranges of about this many points, at least kHostChunks and at most kHostChunksMax of them.
+constexpr int64_t kHostChunkPoints = 3414;
+constexpr int kHostChunksMax = kMaxHostChunks;
 
 static int host_chunk_count(int64_t P) {
   const int64_t n = (P + kHostChunkPoints - 1) / kHostChunkPoints;

@@ -1069,6 +1069,7 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
   int64_t pc = 0;  // points of the largest range
   for (int64_t n : sizes) pc = n > pc ? n : pc;
   pc = round_up(pc, 32);
+  const int64_t pp = round_up(P, 32);
   if (5 * pc > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
   qmckl_exit_code_device rc = ensure_tables(ctx, c);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -1081,9 +1082,9 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
   void* perm = ao.point_perm;
   void* keys = ao.point_keys;
   void* counts = ao.cell_counts;
-  const bool ok = ensure_raw(ctx, &perm, &ao.perm_cap, sizeof(int32_t) * pc) &&
-                  ensure_raw(ctx, &keys, &ao.keys_cap, sizeof(int32_t) * pc) &&
-                  ensure_raw(ctx, &counts, &ao.counts_cap, sizeof(int32_t) * kOrderCells);
+  const bool ok = ensure_raw(ctx, &perm, &ao.perm_cap, sizeof(int32_t) * pp) &&
+                  ensure_raw(ctx, &keys, &ao.keys_cap, sizeof(int32_t) * pp) &&
+                  ensure_raw(ctx, &counts, &ao.counts_cap, sizeof(int32_t) * kOrderCells * (size_t)nc);
   ao.point_perm = static_cast<int32_t*>(perm);
   ao.point_keys = static_cast<int32_t*>(keys);
   ao.cell_counts = static_cast<int32_t*>(counts);
@@ -1100,36 +1101,47 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
       return fail(c, QMCKL_FAILURE_DEVICE, fn, "event creation failed");
     }
   __nv_bfloat16* ap = static_cast<__nv_bfloat16*>(mo.ao_split);
-  // the ranges' jobs, encoded and uploaded once for this shape and these buffers
+  // the ranges' jobs and first points, encoded and uploaded once for this shape and these buffers
+  // (range k's processing order lives at point_perm + its first point)
   HostChunkJobs& hj = mo.host_jobs;
   const HostChunkKey key{P, M, kp, nc, ratio, ap, mo.coef_split, mo.mo_vgl, ao.point_perm};
+  const size_t job_bytes = sizeof(SplitJob) * (size_t)nc;
   if (!(hj.key == key) || !hj.jobs) {
     hj.key = HostChunkKey{};
-    if (!ensure_raw(ctx, &hj.jobs, &hj.jobs_cap, sizeof(SplitJob) * (size_t)nc))
+    if (!ensure_raw(ctx, &hj.jobs, &hj.jobs_cap, job_bytes + sizeof(int64_t) * (size_t)(nc + 1)))
       return fail(c, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "split job descriptors");
     std::vector<SplitJob> jobs((size_t)nc);
+    std::vector<int64_t> bounds((size_t)nc + 1);
     int64_t off = 0;
     for (int k = 0; k < nc; ++k) {
       const int64_t n = sizes[k];
-      hj.tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 32), n, ao.point_perm,
+      bounds[k] = off;
+      hj.tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 32), n, ao.point_perm + off,
                                 static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
       if (hj.tiles[k] < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
       off += n;
     }
-    if (cudaMemcpy(hj.jobs, jobs.data(), sizeof(SplitJob) * (size_t)nc, cudaMemcpyHostToDevice) != cudaSuccess) {
+    bounds[nc] = off;
+    unsigned char* dst = static_cast<unsigned char*>(hj.jobs);
+    if (cudaMemcpy(dst, jobs.data(), job_bytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(dst + job_bytes, bounds.data(), sizeof(int64_t) * bounds.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
       cudaGetLastError();
       return fail(c, QMCKL_FAILURE_DEVICE, fn, "job upload failed");
     }
     hj.key = key;
   }
   const SplitJob* d_jobs = static_cast<const SplitJob*>(hj.jobs);
-  cudaError_t e = cudaSuccess;
+  const int64_t* d_bounds = reinterpret_cast<const int64_t*>(static_cast<const unsigned char*>(hj.jobs) + job_bytes);
+  // every range's processing order in one pass (three launches instead of three per range)
+  cudaError_t e = launch_point_order_ranges(ctx, ao.tables, ctx->point.coord, P, d_bounds, nc, ao.point_keys,
+                                            ao.cell_counts, ao.point_perm);
   int64_t off = 0;
   for (int k = 0; k < nc && e == cudaSuccess; ++k) {
     const int64_t n = sizes[k];
     const double* coord = ctx->point.coord + off;  // rows of [3][P], slice of n points
-    launch_point_order(ctx, ao.tables, coord, P, n, ao.point_keys, ao.cell_counts, ao.point_perm);
-    launch_ao_planes(ctx, ao.tables, coord, P, ao.point_perm, n, kp, ap);
+    e = launch_ao_planes(ctx, ao.tables, coord, P, ao.point_perm + off, n, kp, ap);
+    if (e != cudaSuccess) break;
     {
       LaunchScope scope(ctx, "mo_vgl_split_bf16");
       e = launch_split_jobs(ctx->stream, d_jobs + k, 1, hj.tiles[k], err, ctl_of(ctx));
