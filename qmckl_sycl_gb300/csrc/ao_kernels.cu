@@ -509,29 +509,12 @@ __device__ __forceinline__ void shell_generic(Writer<O>& w, double x, double y, 
 // One warp task: 32 points (lane = point) x one chunk of consecutive nuclei. G: the basis has
 // shells with l >= 4 (the generic path is compiled in only then, since its local arrays and
 // extra live values cost the common kernel registers).
-template <Out O, bool G, bool B>
-__device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
-                                        const double* __restrict__ thi, const double* __restrict__ tlo,
-                                        const double* __restrict__ fine, double* __restrict__ ebuf, int lane) {
+template <Out O, bool G, bool B, bool S>
+__device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, const NucleusChunk* chunk,
+                                           Stage<ncomp<O>()>* st, const double* __restrict__ thi,
+                                           const double* __restrict__ tlo, const double* __restrict__ fine,
+                                           double* __restrict__ ebuf, int lane) {
   constexpr int NC = ncomp<O>();
-  // the task's segment (the last one starting at or before it), selected with constant indices
-  // so that the kernel-parameter arrays are read in place
-  int64_t t0 = a.seg_task[0], g0 = a.seg_group[0];
-  const NucleusChunk* c0 = a.seg_chunks[0];
-  int cn = a.seg_chunk_num[0];
-#pragma unroll
-  for (int k = 1; k < FusedArgs::kMaxSegments; ++k) {
-    if (k < a.nseg && task >= a.seg_task[k]) {
-      t0 = a.seg_task[k];
-      g0 = a.seg_group[k];
-      c0 = a.seg_chunks[k];
-      cn = a.seg_chunk_num[k];
-    }
-  }
-  const int64_t t = task - t0;
-  const int64_t g = t / cn;
-  const int64_t group = g0 + g;
-  const NucleusChunk* chunk = c0 + (t - g * cn);
   const int64_t p0 = group * 32;
   const int64_t remaining = a.point_num - p0;
   const int nvalid = remaining < 32 ? (int)remaining : 32;
@@ -545,8 +528,14 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
 
   for (int n = cj.nucl_begin; n < cj.nucl_end; ++n) {
     const NucleusEntry& N = a.nuclei[n];
-    // the nucleus's shells, or the chunk's part of them (a piece)
-    const int s_begin = max(N.shell_begin, cj.shell_lo), s_end = min(N.shell_end, cj.shell_hi);
+    // the nucleus's shells, or with S the chunk's part of them (a piece). Compiled in only where
+    // pieces are used: the clamped bounds cost the batch kernel 40 % (2.27 -> 3.18 ms on the
+    // 64-molecule batch's planes)
+    int s_begin = N.shell_begin, s_end = N.shell_end;
+    if constexpr (S) {
+      s_begin = max(s_begin, cj.shell_lo);
+      s_end = min(s_end, cj.shell_hi);
+    }
     const double x = ex - N.x, y = ey - N.y, z = ez - N.z;
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
     const uint64_t r2b = bits_of(r2);
@@ -561,9 +550,13 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
     const bool scr = r2b - N.screen_bits - 1ull < 0x7FF0000000000000ull - N.screen_bits;
     const bool nan_warp = __any_sync(kFull, nanr);  // warp-uniform: the NaN fix-up below costs a branch
     if (__all_sync(kFull, scr)) {
-      const int ao_lo = s_begin == N.shell_begin ? N.ao_begin : a.shells[s_begin].ao_begin;
-      const int ao_hi = s_end == N.shell_end ? N.ao_end : a.shells[s_end].ao_begin;
-      w.emit_zeros(ao_hi - ao_lo);
+      if constexpr (S) {
+        const int ao_lo = s_begin == N.shell_begin ? N.ao_begin : a.shells[s_begin].ao_begin;
+        const int ao_hi = s_end == N.shell_end ? N.ao_end : a.shells[s_end].ao_begin;
+        w.emit_zeros(ao_hi - ao_lo);
+      } else {
+        w.emit_zeros(N.ao_end - N.ao_begin);
+      }
       continue;
     }
     float xf = 0.f, yf = 0.f, zf = 0.f, r2f = 0.f;
@@ -715,6 +708,30 @@ __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<
   w.flush();
 }
 
+// Task `task` of a single-molecule launch: its segment (the last one starting at or before it,
+// selected with constant indices so that the kernel-parameter arrays are read in place), then
+// its point group and chunk.
+template <Out O, bool G, bool B, bool S>
+__device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
+                                        const double* __restrict__ thi, const double* __restrict__ tlo,
+                                        const double* __restrict__ fine, double* __restrict__ ebuf, int lane) {
+  int64_t t0 = a.seg_task[0], g0 = a.seg_group[0];
+  const NucleusChunk* c0 = a.seg_chunks[0];
+  int cn = a.seg_chunk_num[0];
+#pragma unroll
+  for (int k = 1; k < FusedArgs::kMaxSegments; ++k) {
+    if (k < a.nseg && task >= a.seg_task[k]) {
+      t0 = a.seg_task[k];
+      g0 = a.seg_group[k];
+      c0 = a.seg_chunks[k];
+      cn = a.seg_chunk_num[k];
+    }
+  }
+  const int64_t t = task - t0;
+  const int64_t g = t / cn;
+  ao_task_at<O, G, B, S>(a, g0 + g, c0 + (t - g * cn), st, thi, tlo, fine, ebuf, lane);
+}
+
 // Dynamic shared memory of the fused kernels: tables, staging buffers (ao_vgl / ao_value), then
 // with shared exponentials one column of ent_cap doubles per lane.
 template <Out O>
@@ -745,7 +762,7 @@ struct CtaSmem {
 // each warp takes the next task from *counter (zeroed before the launch) until none is left,
 // so that every SM gets the same share of the FP64 work whatever the grid's tail.
 // G: shells with l >= 4 exist; B: shared exponentials (a.ent non-null).
-template <Out O, bool G, bool B>
+template <Out O, bool G, bool B, bool S>
 __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(const FusedArgs a,
                                                                               unsigned long long* counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -754,7 +771,7 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(co
   __syncthreads();
   if (!counter) {
     const int64_t task = (int64_t)blockIdx.x * kWarps + warp;
-    if (task < a.task_num) ao_task<O, G, B>(a, task, sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);  // warp-uniform
+    if (task < a.task_num) ao_task<O, G, B, S>(a, task, sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);  // warp-uniform
     return;
   }
   for (;;) {
@@ -762,7 +779,7 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_fused_kernel(co
     if (lane == 0) t = atomicAdd(counter, 1ull);
     t = __shfl_sync(kFull, t, 0);
     if (t >= (unsigned long long)a.task_num) break;
-    ao_task<O, G, B>(a, (int64_t)t, sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);
+    ao_task<O, G, B, S>(a, (int64_t)t, sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);
   }
 }
 
@@ -791,7 +808,10 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
       else hi = mid - 1;
     }
     const FusedArgs& a = mols[lo];  // fields read from global memory as needed (registers)
-    ao_task<O, G, B>(a, task - task_begin[lo], sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);
+    const int64_t local = task - task_begin[lo];  // one segment per molecule
+    const int cn = a.chunk_num;
+    const int64_t g = local / cn;
+    ao_task_at<O, G, B, false>(a, g, a.chunks + (local - g * cn), sm.st, sm.thi, sm.tlo, sm.fine, sm.ebuf, lane);
   }
 }
 
@@ -910,12 +930,16 @@ __global__ void cell_scatter_kernel(const int32_t* __restrict__ keys, int64_t P,
 }
 
 // Picks the first nucleus-chunk level with at least `target` warp tasks; when none has that
-// many, the pieces (level index ao_level_count(t)) if there are more of them.
-int pick_level(const AoTables& t, int64_t groups, int64_t target) {
+// many, the pieces (level index ao_level_count(t)) if allowed and there are more of them. The
+// FP64 outputs do not take pieces as their level: a piece's AO columns start and end inside the
+// 8-AO windows they are stored in, and those partial windows cost more than the balance gains
+// (CHBrClF, 40,960 points: ao_vgl 0.72 ms with pieces against 0.57 ms; the planes kernel, which
+// stores whole 64-byte segments per AO, 0.058 against 0.116 ms).
+int pick_level(const AoTables& t, int64_t groups, int64_t target, bool pieces) {
   const int levels = (int)t.level_offsets.size();
   for (int lv = 0; lv < levels; ++lv)
     if (groups * (int64_t)t.level_sizes[lv] >= target) return lv;
-  return t.piece_num > t.level_sizes[levels - 1] ? levels : levels - 1;
+  return pieces && t.piece_num > t.level_sizes[levels - 1] ? levels : levels - 1;
 }
 
 
@@ -937,24 +961,28 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
   static size_t cached_smem = 0;
   static int cached_per_sm = 0;
   if (cached_smem != smem || cached_per_sm == 0) {
-    cached_per_sm = resident_per_sm(ao_fused_kernel<O, G, B>, smem);
+    cached_per_sm = resident_per_sm(ao_fused_kernel<O, G, B, false>, smem);
     cached_smem = smem;
   }
+  constexpr bool kPieces = O == Out::Planes;  // the FP64 outputs never take pieces (see pick_level)
   const int per_sm = cached_per_sm;
   const int64_t resident_warps = (int64_t)t.sm_count * per_sm * kWarps;
   // two or more tasks per resident warp, taken from a counter: with one task per warp the SMs
   // that receive one CTA more than the others set the time (4 or 5 CTAs per SM on the medium
   // workload, 16 % idle FP64 issue)
-  const int level = pick_level(t, groups, kTasksPerWarp * resident_warps);
+  const int level = pick_level(t, groups, kTasksPerWarp * resident_warps, kPieces);
   FusedArgs a = make_fused_args(t, level, coord, perm, point_num, out, planes, row_len);
-  // the last tasks at ever finer levels down to the pieces: a warp's last task is short, so the
-  // launch ends with every warp busy nearly to the end (a task at the coarse level takes ~1/3
-  // of the launch, and a lone warp runs a nucleus's FP64 work on one sub-partition's FP64 unit).
-  // Measured on the medium workload's planes (40,960 points): 0.982 ms against 1.005 ms for one
-  // segment; with about 4 or 16 times as many tail tasks 1.010 / 1.062 ms, and with 4, 8 or 32
-  // tasks per warp at the coarse level 1.05 / 1.09 / 1.36 ms (finer tasks cost more than they
-  // balance: every task takes a global counter and reloads its points).
-  plan_segments(a, t, level, resident_warps, kTailSegments);
+  // the last tasks at ever finer nucleus-chunk levels: a warp's last task is short, so the launch
+  // ends with every warp busy nearly to the end (a task at the coarse level takes ~1/3 of the
+  // launch, and a lone warp runs a nucleus's FP64 work on one sub-partition's FP64 unit).
+  // Measured on the medium workload's planes (40,960 points): 0.968 ms against 1.005 ms for one
+  // segment; ending with pieces too 0.980 ms (the kernel with clamped shell ranges is slower);
+  // with about 4 or 16 times as many tail tasks 1.010 / 1.062 ms, and with 4, 8 or 32 tasks per
+  // warp at the coarse level 1.05 / 1.09 / 1.36 ms (finer tasks cost more than they balance:
+  // every task takes a global counter and reloads its points).
+  plan_segments(a, t, level, resident_warps, kTailSegments, false);
+  bool pieces = false;  // some task evaluates a piece of a nucleus: the kernel with clamped shell ranges
+  for (int i = 0; i < a.nseg; ++i) pieces = pieces || a.seg_chunks[i] == t.chunks + t.piece_offset;
   if (coord_ld >= 0) a.coord_ld = coord_ld;
   a.ent = B ? t.ent : nullptr;
   a.ent_cap = B ? t.ent_cap : 0;
@@ -969,9 +997,16 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
     if (e != cudaSuccess) return e;
     blocks = (int64_t)t.sm_count * per_sm;
   }
-  cudaFuncSetAttribute(ao_fused_kernel<O, G, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   LaunchScope scope(ctx, name);
-  ao_fused_kernel<O, G, B><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a, counter);
+  if constexpr (kPieces) {
+    if (pieces) {
+      cudaFuncSetAttribute(ao_fused_kernel<O, G, B, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      ao_fused_kernel<O, G, B, true><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a, counter);
+      return cudaGetLastError();
+    }
+  }
+  cudaFuncSetAttribute(ao_fused_kernel<O, G, B, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  ao_fused_kernel<O, G, B, false><<<(unsigned)blocks, kWarps * 32, smem, ctx->stream>>>(a, counter);
   return cudaGetLastError();
 }
 
@@ -1120,7 +1155,7 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   return a;
 }
 
-void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_tasks, int max_segments) {
+void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_tasks, int max_segments, bool pieces) {
   const int64_t groups = (a.point_num + 31) / 32;
   if (max_segments > FusedArgs::kMaxSegments) max_segments = FusedArgs::kMaxSegments;
   // finer partitions from the finest up: the pieces, then the levels finer than a's
@@ -1129,7 +1164,7 @@ void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_task
     int num;
   };
   std::vector<Part> finer;
-  if (t.piece_num > a.chunk_num) finer.push_back(Part{t.chunks + t.piece_offset, t.piece_num});
+  if (pieces && t.piece_num > a.chunk_num) finer.push_back(Part{t.chunks + t.piece_offset, t.piece_num});
   for (int lv = (int)t.level_offsets.size() - 1; lv > level; --lv)
     if (t.level_sizes[lv] > a.chunk_num && (finer.empty() || t.level_sizes[lv] < finer.back().num))
       finer.push_back(Part{t.chunks + t.level_offsets[lv], t.level_sizes[lv]});

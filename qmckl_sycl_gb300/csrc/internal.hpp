@@ -460,10 +460,11 @@ int ao_level_count(const AoTables& t);
 bool ao_shared_exponentials(const AoTables& t, bool planes);
 FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, const int32_t* perm, int64_t point_num,
                           double* out, void* planes, int64_t row_len);
-// Ends a's schedule with finer segments: from the pieces up through the levels finer than a's,
-// each holding about tail_tasks tasks, at most max_segments segments in all and at most half of
-// the point groups in the finer ones.
-void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_tasks, int max_segments);
+// Ends a's schedule with finer segments: from the pieces (when `pieces`) up through the levels
+// finer than a's, each holding about tail_tasks tasks, at most max_segments segments in all and at
+// most half of the point groups in the finer ones.
+void plan_segments(FusedArgs& a, const AoTables& t, int level, int64_t tail_tasks, int max_segments,
+                   bool pieces);
 // Persistent AO kernel over the tasks of nmol molecules: mols[m]'s tasks are numbered from
 // task_begin[m] (non-decreasing, task_begin[nmol] = total); warps take tasks from *counter
 // (zeroed before the launch). planes selects the BF16-plane output; high_l must be set when
