@@ -21,6 +21,7 @@
 //   :962-965) and a NULL file handle QMCKL_INVALID_ARG_2_DEVICE (the reference asserts).
 #include <dlfcn.h>
 
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
@@ -154,22 +155,42 @@ qmckl_exit_code_device io_fail(qmckl_context_device context, const TrexioApi* ap
   return fail(context, QMCKL_FAILURE_DEVICE, what, api->string_of_error(rcio));
 }
 
+// A zero-filled host array from calloc: an allocation that fails (a file that declares absurd
+// sizes) leaves it empty and returns false instead of throwing across the C ABI.
+template <class T>
+struct Array {
+  T* p = nullptr;
+  Array() = default;
+  Array(const Array&) = delete;
+  Array& operator=(const Array&) = delete;
+  ~Array() { free(p); }
+  bool resize(int64_t n) {
+    free(p);
+    p = nullptr;
+    if (n < 0 || (uint64_t)n > (uint64_t)(PTRDIFF_MAX / sizeof(T))) return false;
+    p = static_cast<T*>(calloc(n > 0 ? (size_t)n : 1, sizeof(T)));
+    return p != nullptr;
+  }
+  T* data() { return p; }
+  T& operator[](int64_t i) { return p[i]; }
+  const T& operator[](int64_t i) const { return p[i]; }
+};
+
 // Inverts a member -> owner map (TREXIO's basis.nucleus_index per shell, basis.shell_index per
 // primitive) into each owner's first member and member count. Fails when an owner is out of
 // [0, owner_num) or its members are not contiguous.
-bool group_members(const std::vector<int64_t>& owner, int64_t owner_num, std::vector<int64_t>* first,
-                   std::vector<int64_t>* count) {
-  first->assign((size_t)owner_num, 0);
-  count->assign((size_t)owner_num, 0);
-  for (size_t i = 0; i < owner.size(); ++i) {
+bool group_members(const Array<int64_t>& owner, int64_t member_num, int64_t owner_num, Array<int64_t>* first,
+                   Array<int64_t>* count) {
+  for (int64_t k = 0; k < owner_num; ++k) (*first)[k] = (*count)[k] = 0;
+  for (int64_t i = 0; i < member_num; ++i) {
     const int64_t k = owner[i];
     if (k < 0 || k >= owner_num) return false;
-    if ((*count)[(size_t)k] == 0) {
-      (*first)[(size_t)k] = (int64_t)i;
+    if ((*count)[k] == 0) {
+      (*first)[k] = i;
     } else if (owner[i - 1] != k) {
       return false;  // k's members resume after another owner's
     }
-    (*count)[(size_t)k] += 1;
+    (*count)[k] += 1;
   }
   return true;
 }
@@ -203,13 +224,14 @@ qmckl_exit_code_device qmckl_trexio_read_nucleus_X_device(qmckl_context_device c
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_nucleus_num", rcio);
   rc = qmckl_set_nucleus_num_device(context, n);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
-  std::vector<double> charge((size_t)n);
+  Array<double> charge, coord;
+  if (n > INT64_MAX / 3 || !charge.resize(n) || !coord.resize(3 * n))
+    return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, "qmckl_trexio_read_nucleus_X_device", nullptr);
   rcio = api->nucleus_charge(file, charge.data(), n);
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_nucleus_charge", rcio);
   rc = qmckl_set_nucleus_charge_device(context, charge.data(), n);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
-  std::vector<double> coord((size_t)(3 * n));  // TREXIO's [nucleus][3]
-  rcio = api->nucleus_coord(file, coord.data(), 3 * n);
+  rcio = api->nucleus_coord(file, coord.data(), 3 * n);  // TREXIO's [nucleus][3]
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_nucleus_coord", rcio);
   return qmckl_set_nucleus_coord_device(context, 'N', coord.data(), 3 * n);
 }
@@ -246,27 +268,33 @@ qmckl_exit_code_device qmckl_trexio_read_ao_X_device(qmckl_context_device contex
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
 
   // shells per nucleus from the nucleus of each shell (:229-420)
-  std::vector<int64_t> owner((size_t)shell_num), first, count;
+  const char* fn = "qmckl_trexio_read_ao_X_device";
+  Array<int64_t> owner, first, count;
+  Array<int32_t> ang_mom;
+  Array<double> values;
+  if (!owner.resize(shell_num) || !first.resize(nucl_num) || !count.resize(nucl_num))
+    return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, fn, nullptr);
   rcio = api->nucleus_index(file, owner.data(), shell_num);
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_basis_nucleus_index", rcio);
-  if (!group_members(owner, nucl_num, &first, &count))
+  if (!group_members(owner, shell_num, nucl_num, &first, &count))
     return fail(context, QMCKL_FAILURE_DEVICE, "trexio_read_basis_nucleus_index", "Irrelevant data in TREXIO file");
   rc = qmckl_set_ao_basis_nucleus_index_device(context, first.data(), nucl_num);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
   rc = qmckl_set_ao_basis_nucleus_shell_num_device(context, count.data(), nucl_num);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
 
-  std::vector<int32_t> ang_mom((size_t)shell_num);
+  if (!ang_mom.resize(shell_num)) return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, fn, nullptr);
   rcio = api->shell_ang_mom(file, ang_mom.data(), shell_num);
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_basis_shell_ang_mom", rcio);
   rc = qmckl_set_ao_basis_shell_ang_mom_device(context, ang_mom.data(), shell_num);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
 
   // primitives per shell from the shell of each primitive (:460-640)
-  owner.assign((size_t)prim_num, 0);
+  if (!owner.resize(prim_num) || !first.resize(shell_num) || !count.resize(shell_num))
+    return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, fn, nullptr);
   rcio = api->shell_index(file, owner.data(), prim_num);
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_basis_shell_prim_num", rcio);
-  if (!group_members(owner, shell_num, &first, &count))
+  if (!group_members(owner, prim_num, shell_num, &first, &count))
     return fail(context, QMCKL_FAILURE_DEVICE, "trexio_read_basis_shell_prim_num", "Irrelevant data in TREXIO file");
   rc = qmckl_set_ao_basis_shell_prim_num_device(context, count.data(), shell_num);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -285,9 +313,8 @@ qmckl_exit_code_device qmckl_trexio_read_ao_X_device(qmckl_context_device contex
       {api->prim_factor, prim_num, qmckl_set_ao_basis_prim_factor_device, "trexio_read_basis_prim_factor"},
       {api->ao_normalization, ao_num, qmckl_set_ao_basis_ao_factor_device, "trexio_read_ao_normalization"},
   };
-  std::vector<double> values;
   for (const Dset& d : dsets) {
-    values.assign((size_t)d.num, 0.0);
+    if (!values.resize(d.num)) return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, fn, nullptr);
     rcio = d.read(file, values.data(), d.num);
     if (rcio != kTrexioSuccess) return io_fail(context, api, d.what, rcio);
     rc = d.set(context, values.data(), d.num);
@@ -309,7 +336,9 @@ qmckl_exit_code_device qmckl_trexio_read_mo_X_device(qmckl_context_device contex
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_mo_num", rcio);
   rc = qmckl_set_mo_basis_mo_num_device(context, mo_num);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
-  std::vector<double> coef((size_t)(ao_num * mo_num));  // TREXIO's [mo][ao]
+  Array<double> coef;  // TREXIO's [mo][ao]
+  if (mo_num > INT64_MAX / ao_num || !coef.resize(ao_num * mo_num))
+    return fail(context, QMCKL_ALLOCATION_FAILED_DEVICE, "qmckl_trexio_read_mo_X_device", nullptr);
   rcio = api->mo_coefficient(file, coef.data(), ao_num * mo_num);
   if (rcio != kTrexioSuccess) return io_fail(context, api, "trexio_read_mo_coefficient", rcio);
   return qmckl_set_mo_basis_coefficient_device(context, coef.data());

@@ -26,7 +26,7 @@ def _asan_env(**extra):
     libasan = subprocess.run(["gcc", "-print-file-name=libasan.so"], capture_output=True, text=True).stdout.strip()
     if not os.path.isabs(libasan) or not os.path.exists(libasan):
         pytest.skip("libasan not available")
-    env = dict(os.environ, LD_PRELOAD=libasan, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1:protect_shadow_gap=0",
+    env = dict(os.environ, LD_PRELOAD=libasan, ASAN_OPTIONS="detect_leaks=0:halt_on_error=1:protect_shadow_gap=0:allocator_may_return_null=1",
                UBSAN_OPTIONS="halt_on_error=1:print_stacktrace=1", **extra)
     return env
 

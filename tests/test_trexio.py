@@ -164,3 +164,16 @@ def test_group_conversion_matches_the_fixture(chbrclf):
     assert all(int(np.argmax(sn == k)) == chbrclf.nucleus_index[k] for k in range(chbrclf.nucl_num))
     ps = r["basis_shell_index"]
     assert (np.bincount(ps, minlength=chbrclf.shell_num) == chbrclf.shell_prim_num).all()
+
+
+def test_absurd_sizes_fail_cleanly(use_double, ctx, tmp_path):
+    # a file that declares 10^15 shells: the reader reports an allocation failure instead of
+    # throwing across the C ABI
+    L = capi.lib()
+    L.qmckl_set_nucleus_num_device(ctx, 2)
+    f = _open(_basis_file(tmp_path, [0, 1], [0, 1], name="big.trexio", basis_shell_num=np.int64(10**15),
+                          basis_prim_num=np.int64(10**15), ao_num=np.int64(10**15)))
+    assert L.qmckl_trexio_read_ao_X_device(ctx, f) == 104
+    assert error_of(ctx)[:2] == (104, "qmckl_trexio_read_ao_X_device")
+    use_double.trexio_close.argtypes = [ctypes.c_void_p]
+    use_double.trexio_close(f)
