@@ -210,15 +210,14 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
 // the AO kernel's finest tasks (pieces of nuclei), so the per-range cost is small and many ranges
 // pay: the first range, whose compute the link waits for, stays short. Measured end to end
 // (set_point from and mo_vgl into page-locked host memory, ms per step; the link alone needs
-// 2.55 / 10.2 / 63.6 ms): 40,960 points 3.14 / 3.01 / 2.94 / 2.91 / 2.87 / 2.87 / 3.01 ms with
-// 4 / 6 / 8 / 10 / 12 / 14 / 16 ranges; 163,840 points 11.19 / 10.98 / 10.84 / 10.73 / 10.67 ms
-// with 8 / 12 / 16 / 24 / 32; 1,024,000 points 66.6 / 65.8 / 65.4 ms with 16 / 24 / 32. Ranges of
-// unequal size measured slower (a small first range runs its kernels far below the full-size
-// rates).
+// 2.55 / 10.2 / 63.6 ms): 40,960 points 2.91 / 2.89 / 2.85 / 2.84 / 2.84 ms with 8 / 10 / 12 / 14 /
+// 16 ranges; 163,840 points 11.19 / 10.98 / 10.84 / 10.73 / 10.67 ms with 8 / 12 / 16 / 24 / 32;
+// 1,024,000 points 66.6 / 65.8 / 65.4 ms with 16 / 24 / 32. Ranges of unequal size measured
+// slower (a small first range runs its kernels far below the full-size rates).
 constexpr int kHostChunks = 6;
 constexpr double kHostChunkRatio = 1.0;
 // Ranges of about this many points, at least kHostChunks and at most kHostChunksMax of them.
-constexpr int64_t kHostChunkPoints = 3414;
+constexpr int64_t kHostChunkPoints = 2926;
 constexpr int kHostChunksMax = kMaxHostChunks;
 
 static int host_chunk_count(int64_t P) {
