@@ -307,6 +307,7 @@ struct ShellVals {
   double R;    // radial value t0
   double t1, t2, t3;  // radial gradient = g * (x, y, z)
   double Rt;   // t4 + 2 l g, the radial part of the Laplacian after Euler's identity
+  double R2, R6;  // 2 R and 6 R (split-BF16 form, shells with l = 2 and 3)
   float Rf, t1f, t2f, t3f;  // FP32 copies for the split-BF16 form's value and gradient
 };
 
@@ -377,10 +378,21 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
     float v0 = Pf * s.Rf;
     const double yz = Y[b] * Z[c];
     const double P = X[a] * yz;
-    double lap = P * s.Rt;
-    if constexpr (a > 1) lap = fma((double)(a * (a - 1)) * X[a - 2], yz * s.R, lap);
-    if constexpr (b > 1) lap = fma((double)(b * (b - 1)) * Y[b - 2], (X[a] * Z[c]) * s.R, lap);
-    if constexpr (c > 1) lap = fma((double)(c * (c - 1)) * Z[c - 2], (X[a] * Y[b]) * s.R, lap);
+    // l <= 3: at most one exponent e of a, b, c is 2 or more, so the polynomial's second
+    // derivatives add one term e (e - 1) x^(e-2) m R, with m the other two coordinates' powers
+    // (1, x, y or z) and x^(e-2) = 1 or the coordinate itself: lap = fma(P, Rt, (e (e - 1) R) m),
+    // e (e - 1) R formed once per shell (2R, 6R), all in FP64
+    static_assert(a + b + c <= 3, "the fixed-l path covers l <= 3");
+    double lap;
+    if constexpr (a > 1) {
+      lap = fma(P, s.Rt, (a == 2 ? s.R2 : s.R6) * (X[a - 2] * yz));
+    } else if constexpr (b > 1) {
+      lap = fma(P, s.Rt, (b == 2 ? s.R2 : s.R6) * (Y[b - 2] * (X[a] * Z[c])));
+    } else if constexpr (c > 1) {
+      lap = fma(P, s.Rt, (c == 2 ? s.R2 : s.R6) * (Z[c - 2] * (X[a] * Y[b])));
+    } else {
+      lap = P * s.Rt;
+    }
     if (!is_one(f)) {
       const float ff = f64_to_f32(f);
       v0 *= ff;
@@ -432,8 +444,13 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
 // Components of one shell in the reference's order: a descending, then b descending
 // (src/qmckl_ao_sycl.cpp:297-305).
 template <Out O, int L>
-__device__ __forceinline__ void shell_fixed(Writer<O>& w, const Pows& pw, const ShellVals& s,
+__device__ __forceinline__ void shell_fixed(Writer<O>& w, const Pows& pw, const ShellVals& sv_in,
                                             const double* __restrict__ aof, int ao0, bool zero) {
+  ShellVals s = sv_in;
+  if constexpr (O == Out::Planes && L >= 2) {
+    s.R2 = s.R + s.R;  // exact
+    if constexpr (L >= 3) s.R6 = 3.0 * s.R2;
+  }
   if constexpr (L == 0) {
     cart<O, 0, 0, 0>(w, pw, s, __ldg(aof + ao0), zero);
   } else if constexpr (L == 1) {
