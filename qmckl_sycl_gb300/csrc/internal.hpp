@@ -221,7 +221,7 @@ struct AoBasisData {
 
 // The host-buffer path's contraction jobs (one per point range), kept on the device while the
 // shape and buffers they were encoded for stay the same.
-constexpr int kMaxHostChunks = 32;
+constexpr int kMaxHostChunks = 64;
 struct HostChunkKey {
   int64_t P = 0, M = 0, kp = 0;
   int chunks = 0;
@@ -515,8 +515,9 @@ int split_make_job_mn(void* job_host, const void* a_planes, int64_t pp, int64_t 
                       const void* b_planes, int64_t M, int64_t kp, double* out, int tile_begin, int n_cap);
 cudaError_t split_launch_jobs(cudaStream_t stream, const void* jobs, int njobs, int total_tiles, int* err);
 int64_t split_k_pad(int64_t ao_num);
-// mo_vgl of the split-BF16 form computed in `chunks` point ranges whose results are copied to the
-// host buffer while the next range computes (the cache ends up holding the full result).
+// mo_vgl of the split-BF16 form computed in point ranges whose results are copied to the host
+// buffer while the next range computes (the cache ends up holding the full result): `chunks`
+// ranges growing by `ratio`, or with chunks = 0 ranges sized by the contraction's waves.
 qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, double* host_dst, int chunks,
                                             double ratio);
 // The member's coefficient planes for the split-BF16 form (built once per coefficient set)

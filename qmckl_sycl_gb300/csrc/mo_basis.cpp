@@ -205,25 +205,17 @@ qmckl_exit_code_device qmckl_provide_mo_basis_mo_value_device(qmckl_context_devi
   return QMCKL_SUCCESS_DEVICE;
 }
 
-// Point ranges of the host-buffer path and their size ratio (1: equal ranges). All ranges are
-// put in processing order by one pass before the first range computes, and small ranges take
-// the AO kernel's finest tasks (pieces of nuclei), so the per-range cost is small and many ranges
-// pay: the first range, whose compute the link waits for, stays short. Measured end to end
-// (set_point from and mo_vgl into page-locked host memory, ms per step; the link alone needs
-// 2.55 / 10.2 / 63.6 ms): 40,960 points 2.91 / 2.89 / 2.85 / 2.84 / 2.84 ms with 8 / 10 / 12 / 14 /
-// 16 ranges; 163,840 points 11.19 / 10.98 / 10.84 / 10.73 / 10.67 ms with 8 / 12 / 16 / 24 / 32;
-// 1,024,000 points 66.6 / 65.8 / 65.4 ms with 16 / 24 / 32. Ranges of unequal size measured
-// slower (a small first range runs its kernels far below the full-size rates).
-constexpr int kHostChunks = 6;
+// Point ranges of the host-buffer path: by default sized by the contraction's waves (each range's
+// tiles fill one wave of the SMs; chunks = 0), so that no range's contraction ends with idle SMs.
+// All ranges are put in processing order by one pass before the first range computes, and small
+// ranges take the AO kernel's finest tasks (pieces of nuclei), so the per-range cost is small and
+// many ranges pay: the first range, whose compute the link waits for, stays short. Measured end
+// to end on 40,960 points (set_point from and mo_vgl into page-locked host memory, ms per step; the
+// link alone needs 2.55 ms) with equal ranges: 2.91 / 2.89 / 2.86 / 2.85 / 2.84 / 2.84 / 2.84 /
+// 3.15 / 2.79 ms with 8 / 10 / 11 / 12 / 13 / 14 / 16 / 21 / 22 ranges: 22 ranges of 1888 points
+// make 148 tiles each (one wave of 152 SMs), 21 of 1952 points 154 (a wave and 2 tiles).
+constexpr int kHostChunks = 0;
 constexpr double kHostChunkRatio = 1.0;
-// Ranges of about this many points, at least kHostChunks and at most kHostChunksMax of them.
-constexpr int64_t kHostChunkPoints = 2926;
-constexpr int kHostChunksMax = kMaxHostChunks;
-
-static int host_chunk_count(int64_t P) {
-  const int64_t n = (P + kHostChunkPoints - 1) / kHostChunkPoints;
-  return (int)(n < kHostChunks ? kHostChunks : (n > kHostChunksMax ? kHostChunksMax : n));
-}
 
 // QMCKL_GB300_HOST_CHUNKS="<ranges>[,<ratio>]" overrides the plan (for measurements).
 static void host_chunk_plan_override(int* chunks, double* ratio) {
@@ -257,10 +249,10 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_vgl_device(qmckl_context_device con
   if (mo.provided && ctx->ao_basis.provided && ctx->precision == QMCKL_PRECISION_SPLIT_BF16_DEVICE &&
       ctx->point.date > mo.mo_vgl_date && ctx->point.num >= 16384 && mo_vgl &&
       size_max >= 5 * ctx->point.num * mo.mo_num && ensure_device(ctx) && host_memory(mo_vgl)) {
-    // equal point ranges (QMCKL_GB300_HOST_CHUNKS="<ranges>,<ratio>" overrides the plan); the
-    // device-to-host link (~193 GB/s) needs 2.54 ms for the medium workload's 491 MB of mo_vgl,
-    // the computation 1.73 ms
-    int chunks = host_chunk_count(ctx->point.num);
+    // point ranges sized by the contraction's waves (QMCKL_GB300_HOST_CHUNKS="<ranges>,<ratio>"
+    // overrides the plan); the device-to-host link (~193 GB/s) needs 2.54 ms for the medium
+    // workload's 491 MB of mo_vgl, the computation 1.53 ms
+    int chunks = kHostChunks;
     double ratio = kHostChunkRatio;
     host_chunk_plan_override(&chunks, &ratio);
     qmckl_exit_code_device rc = split_mo_vgl_to_host(ctx, context, mo_vgl, chunks, ratio);

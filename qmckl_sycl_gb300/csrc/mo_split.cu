@@ -1034,6 +1034,26 @@ void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
 
 // Point ranges of the host-buffer path: sizes in the ratio 1 : ratio : ratio^2 ... (ratio 1: equal
 // ranges), multiples of 32 points, the last range taking the rest.
+// Ranges sized by the contraction's waves: each range but the last has the most points (a
+// multiple of 32) whose tiles fill `waves` waves of one tile per SM, with waves = 1 unless that
+// needs more than max_ranges ranges; the last range takes the rest. A range whose tiles end a
+// wave exactly leaves no SM idle at its end: on the medium workload (M = 300, two column tiles
+// of 150) ranges of 1920 points, 150 tiles each.
+std::vector<int64_t> wave_plan(int64_t P, int64_t M, int sms, int max_ranges) {
+  const int64_t col_tiles = (M + tile_cols(M) - 1) / tile_cols(M);
+  int64_t n = 32;
+  for (int64_t waves = 1;; ++waves) {
+    const int64_t row_tiles = waves * sms / col_tiles;  // rows 5 n <= row_tiles * kBM
+    n = row_tiles * kBM / 5 / 32 * 32;
+    if (n >= 32 && (P + n - 1) / n <= max_ranges) break;
+    if (row_tiles * kBM / 5 >= P) break;
+  }
+  if (n < 32) n = 32;
+  std::vector<int64_t> sizes;
+  for (int64_t done = 0; done < P; done += n) sizes.push_back(n < P - done ? n : P - done);
+  return sizes;
+}
+
 std::vector<int64_t> chunk_plan(int64_t P, int chunks, double ratio) {
   std::vector<int64_t> sizes;
   double total = 0.0, w = 1.0;
@@ -1063,8 +1083,17 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
   MoBasisData& mo = ctx->mo_basis;
   AoBasisData& ao = ctx->ao_basis;
   const int64_t kp = round_up(A, kBK);
-  chunks = chunks < 1 ? 1 : (chunks > kMaxHostChunks ? kMaxHostChunks : chunks);
-  const std::vector<int64_t> sizes = chunk_plan(P, chunks, ratio);
+  std::vector<int64_t> sizes;
+  if (chunks > 0) {
+    chunks = chunks > kMaxHostChunks ? kMaxHostChunks : chunks;
+    sizes = chunk_plan(P, chunks, ratio);
+  } else {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    sizes = wave_plan(P, M, sms, kMaxHostChunks);
+    ratio = 0.0;
+  }
   const int nc = (int)sizes.size();
   int64_t pc = 0;  // points of the largest range
   for (int64_t n : sizes) pc = n > pc ? n : pc;
