@@ -115,6 +115,30 @@ def test_host_getter_overlaps_copies_bitwise():
     assert normwise_rel_err(host[idx], ref) <= MIXED_RTOL
 
 
+@pytest.mark.parametrize("mo_num, point_num", [(161, 16411), (97, 20003), (333, 16416)])
+def test_host_getter_wave_sized_ranges_bitwise(mo_num, point_num):
+    # the host-buffer path's ranges are sized by the contraction's tile waves, which depend on the
+    # MO count's column tiles (161: two of 96; 97: one; 333: three of 112); a point count that is
+    # not a multiple of 32 leaves a ragged last range. Every layout gives the one-pass bits.
+    import ctypes
+
+    from qmckl_sycl_gb300.systems import SPDF_WEIGHTS, make_system
+
+    s = make_system(5, 12, 10, 9.0, 160, SPDF_WEIGHTS, 5, (0.05, 60.0), mo_num, point_num, 2.0, name="waves")
+    with Context(0) as ctx:
+        ctx.load_system(s)
+        ctx.set_precision(PRECISION_SPLIT_BF16)
+        P, M = s.point_num, s.mo_num
+        host = ctx.get_mo_vgl(P)
+        dev = ctx.buffer("mo", 8 * 5 * P * M)
+        ctx.call("get_mo_basis_mo_vgl_inplace", dev.ptr, 5 * P * M)
+        one_pass = ctx.download(dev.ptr, (P, 5, M))
+    assert np.array_equal(host, one_pass)
+    idx = np.arange(0, P, 211)
+    ref = oracle.forward(s.with_points(s.coord[idx]), want=("mo_vgl",))["mo_vgl"]
+    assert normwise_rel_err(host[idx], ref) <= MIXED_RTOL
+
+
 def test_split_zero_and_tiny_mo_columns():
     # an MO whose coefficients are all zero gives exact zeros (the epilogue's float-to-double
     # conversion of zeros), an MO scaled by 1e-20 keeps its own relative accuracy (the BF16 terms
