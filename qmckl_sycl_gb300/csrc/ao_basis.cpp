@@ -59,6 +59,32 @@ uint64_t prim_threshold(double expo) {
   return bits_of(c);
 }
 
+// The split-BF16 form's record of one primitive (or, with coef 1, one distinct exponent):
+// -expo as an FP32 pair, |coef| = mant 2^k with ln(mant) = jm L + dh (L = ln 2 / kFine, jm the
+// nearest integer), sign * 2^k as float bits, coef as an FP32 pair. The remainders are formed
+// in long double, then rounded once to float.
+PrimFold fold_entry(double expo, double coef, uint64_t thr_bits) {
+  PrimFold f{};
+  f.thr_bits = thr_bits;
+  f.na = -expo;
+  f.nah = (float)(-expo);
+  f.nal = (float)(-expo - (double)f.nah);  // the difference is exact in double
+  f.ch = (float)coef;
+  f.cl = (float)(coef - (double)f.ch);
+  if (coef != 0.0 && std::isfinite(coef)) {
+    int e2 = 0;
+    const double m = std::frexp(std::fabs(coef), &e2);  // |coef| = m 2^e2, m in [0.5, 1)
+    const int k = e2 - 1;
+    const long double L = logl(2.0L) / (long double)kFine;
+    const long double lnm = logl(2.0L * (long double)m);
+    const long double jm = roundl(lnm / L);
+    f.jm = (int32_t)jm;
+    f.dh = (float)(lnm - jm * L);
+    f.ebase = ((uint32_t)(std::min(std::max(k, -126), 127) + 127) << 23) | (std::signbit(coef) ? 0x80000000u : 0u);
+  }
+  return f;
+}
+
 int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 
 // Per-nucleus exponent tables of src/qmckl_ao_sycl.cpp:855-1065: each nucleus' primitives
@@ -322,31 +348,26 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
     et[0].hi[j] = (double)v;
     et[0].lo[j] = (double)(v - (long double)et[0].hi[j]);
   }
-  for (int j = 0; j < kFine; ++j) et[0].fine[j] = (double)exp2l((long double)j / (long double)kFine);
-  // the split-BF16 form's folded primitives: every exponent positive and finite, every
-  // coefficient zero or of binary exponent within +-900 (so that sign * 2^k * e^y stays a
-  // normal double over the active range y in [-27.7, ln 2))
+  for (int j = 0; j < kFine; ++j) {
+    const long double v = exp2l((long double)j / (long double)kFine);
+    et[0].fine[j].x = (float)v;
+    et[0].fine[j].y = (float)(v - (long double)et[0].fine[j].x);
+  }
+  // the split-BF16 form's folded primitives, evaluated in FP32 pair arithmetic: every exponent
+  // within 2^+-60 (so that -expo and expo r2 over the active range are normal floats) and every
+  // coefficient zero or of binary exponent within +-64 (so that sign * 2^k * e^y, y in
+  // [-27.7, ln 2), and the products of the shared-exponential path stay normal floats)
   bool fold_ok = true;
   t.h_fold.resize(t.h_prims.size());
   for (size_t i = 0; i < t.h_prims.size(); ++i) {
     const PrimEntry& pe = t.h_prims[i];
-    PrimFold& f = t.h_fold[i];
-    f = PrimFold{};
-    if (!(pe.expo > 0.0) || !(pe.expo < 1e150) || !std::isfinite(pe.coef)) fold_ok = false;
-    f.thr_bits = pe.coef == 0.0 ? 0 : pe.thr_bits;
-    f.na = -pe.expo;
-    f.m2a = pe.m2a;
-    f.m2a2 = -2.0 * (pe.expo * pe.expo);
+    if (!(pe.expo >= 0x1p-60) || !(pe.expo <= 0x1p60) || !std::isfinite(pe.coef)) fold_ok = false;
+    t.h_fold[i] = fold_entry(pe.expo, pe.coef, pe.coef == 0.0 ? 0 : pe.thr_bits);
     if (pe.coef != 0.0 && std::isfinite(pe.coef)) {
       int e2 = 0;
-      const double m = std::frexp(std::fabs(pe.coef), &e2);  // |coef| = m 2^e2, m in [0.5, 1)
-      f.k = e2 - 1;
-      f.lnm = std::log(2.0 * m);
-      f.sign = std::signbit(pe.coef) ? 0x80000000u : 0u;
-      if (f.k < -900 || f.k > 900) fold_ok = false;
+      std::frexp(pe.coef, &e2);
+      if (e2 - 1 < -64 || e2 - 1 > 64) fold_ok = false;
     }
-    f.naf = (float)f.na;
-    f.lnmf = (float)f.lnm;
   }
   // point-grouping grid over the nuclei plus a 4-bohr margin, 32 cells along the longest side
   {
@@ -401,13 +422,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
       for (int32_t p = p0; p < p1; ++p) w_all += std::pow(t.h_prims[(size_t)p].expo, -1.5);
       for (double a : ex) {
         w_ent += std::pow(a, -1.5);
-        PrimFold f{};
-        f.thr_bits = prim_threshold(a);
-        f.na = -a;
-        f.m2a = -2.0 * a;
-        f.m2a2 = -2.0 * (a * a);
-        f.naf = (float)f.na;
-        t.h_ent.push_back(f);
+        t.h_ent.push_back(fold_entry(a, 1.0, prim_threshold(a)));
       }
       for (int32_t p = p0; p < p1; ++p)
         t.h_prims[(size_t)p].ent =

@@ -74,8 +74,8 @@ __host__ __device__ constexpr int min_ctas() {
   return O == Out::Planes ? 6 : (O == Out::Vgl ? 5 : 8);
 }
 
-// Dynamic shared memory: the exponential's tables (2 x 32 doubles, plus the 256-entry table
-// of the split-BF16 form), then the per-warp staging buffers.
+// Dynamic shared memory: the exponential's tables (2 x 32 doubles, plus the split-BF16 form's
+// 2048-entry table of FP32 pairs), then the per-warp staging buffers.
 template <Out O>
 __host__ __device__ constexpr size_t stage_offset() {
   return O == Out::Planes ? 512 + 8 * kFine : 512;
@@ -115,45 +115,91 @@ __device__ __forceinline__ double keep_if(bool c, double v) {
   return __longlong_as_double(__double_as_longlong(v) & -(long long)c);
 }
 
-// 2l and 3 + 2l of the radial Laplacian term as doubles, by l (no integer-to-FP64 conversion
-// per shell).
+// 2l of the radial Laplacian term as doubles, by l (no integer-to-FP64 conversion per shell).
 __constant__ double kTwoL[kMaxL + 1] = {0, 2, 4, 6, 8, 10, 12, 14, 16, 18, 20, 22, 24, 26, 28, 30, 32, 34, 36, 38};
-__constant__ double kThreePlusTwoL[kMaxL + 1] = {3, 5, 7, 9, 11, 13, 15, 17, 19, 21, 23, 25, 27, 29, 31, 33, 35, 37, 39, 41};
 
-// -n as a double, exactly, with integer instructions only (n = 0 gives 0).
-__device__ __forceinline__ double neg_int_to_double(int n) {
-  const unsigned u = n < 0 ? 0u - (unsigned)n : (unsigned)n;
-  const int msb = 31 - __clz(u);
-  // the mantissa's leading bit carries into the exponent field: (1022 + msb) + 1
-  const unsigned long long b = ((unsigned long long)(1022 + msb) << 52) + ((unsigned long long)u << (52 - msb));
-  const unsigned long long sg = n > 0 ? 0x8000000000000000ull : 0ull;
-  return __longlong_as_double((long long)((b | sg) & (u == 0 ? 0ull : ~0ull)));
+// ---------------------------------------------------------------- FP32 pair arithmetic
+// The split-BF16 form's radials run on the FP32 pipe (64 times the FP64 rate on this part) as
+// pairs hi + lo of floats carrying about 44 significant bits: products of the high parts made
+// exact with fmaf (the low part of a*b is fmaf(a, b, -a*b)), sums made exact with Knuth's
+// two-sum. The _rn intrinsics are never contracted into fused multiply-adds, which would break
+// these identities.
+struct F2 {
+  float h, l;
+};
+
+// (xh + xl) * (yh + yl) to ~2^-47 relative: xh*yh exactly, the cross terms rounded, xl*yl dropped.
+__device__ __forceinline__ F2 mul_pair(float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float e = fmaf(xh, yh, -p);
+  return {p, fmaf(xh, yl, fmaf(xl, yh, e))};
+}
+
+// s += b: the high parts' sum exactly (two-sum), its error and the low parts into s.l.
+__device__ __forceinline__ void add_pair(F2& s, F2 b) {
+  const float t = __fadd_rn(s.h, b.h);
+  const float bb = __fsub_rn(t, s.h);
+  const float err = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bb)), __fsub_rn(b.h, bb));
+  s.l = __fadd_rn(s.l, __fadd_rn(err, b.l));
+  s.h = t;
+}
+
+// An FP32 value as a double, with integer instructions (normal values and zeros; values below
+// the float normal range become zero, infinities and NaN stay).
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFFu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long mant = (unsigned long long)(u & 0x7FFFFFu) << 29;
+  const unsigned long long ex = e == 0 ? 0ull : (e == 255 ? 0x7FFull : (unsigned long long)(e + 896)) << 52;
+  return __longlong_as_double((long long)(sign | ex | (e == 0 ? 0ull : mant)));
 }
 
 constexpr float kInvLFinef = (float)(kFine / 0.6931471805599453094);  // kFine / ln 2 (picks the index)
-constexpr double kLFine = 0.6931471805599453094 / kFine;  // double nearest ln 2, / kFine (exact)
+constexpr double kLFine = 0.6931471805599453094 / kFine;              // ln 2 / kFine (the double)
+constexpr float kLh = (float)kLFine;                                   // as an FP32 pair
+constexpr float kLm = (float)(kLFine - (double)kLh);
 
-// One primitive of the split-BF16 form: v = coef * e^(-expo r2) = sign * 2^k * e^y with
-// y = ln(mant) - expo r2 in FP64 (one fused multiply-add). e^y = 2^(n>>11) 2^((n&2047)/2048) e^r,
-// r = y - n ln2/2048: n comes from an FP32 estimate of y (|r| <= ln2/4096 + 1.2e-5 on the active
-// range y in [-27.7, ln 2)), -n is formed exactly with integer instructions, e^r - 1 by a
-// degree-3 polynomial (truncation 4e-17), 2^(j/2048) from a 2048-entry table in shared memory,
-// and the power of two and the sign by integer addition: 7 FP64 instructions against 14 for
-// coef * e^-(expo r2) with the 32-entry method. The relative error stays within a few units of
-// 1e-16 |y|.
-__device__ __forceinline__ double fold_value(const PrimFold* __restrict__ F, double r2, float r2f,
-                                             const double* __restrict__ fine) {
-  const float yf = fmaf(__ldg(&F->naf), r2f, __ldg(&F->lnmf));
-  const float tf = fmaf(yf, kInvLFinef, 12582912.0f);  // 1.5 * 2^23: rounds to an integer
-  const int n = __float_as_int(tf) - 0x4B400000;
-  const double y = fma(__ldg(&F->na), r2, __ldg(&F->lnm));
-  const double r = fma(neg_int_to_double(n), kLFine, y);
-  const double p = fma(r * r, fma(r, 1.0 / 6.0, 0.5), r);  // e^r - 1
-  const double th = fine[n & (kFine - 1)];
-  const double e = fma(th, p, th);
-  const unsigned long long m = (unsigned long long)(long long)((n >> kFineBits) + __ldg(&F->k));
-  const unsigned long long b = (unsigned long long)__double_as_longlong(e) + (m << 52);
-  return __longlong_as_double((long long)(b ^ ((unsigned long long)__ldg(&F->sign) << 32)));
+// One primitive of the split-BF16 form, v = coef * e^(-expo r2), as an FP32 pair, for
+// r2 = r2h + r2l (an FP32 pair). With y = -expo r2 + ln(mant) and n = n1 + jm:
+//   e^y = 2^(n >> 11) * 2^((n & 2047)/2048) * e^r,  r = (p - n1 L) + (dh + low parts),
+// where p = fl(-expo r2h) and n1 = round(p / L). t1 = p - n1 Lh is exact (|t1| < 2^-12 and both
+// terms are multiples of 2^-35), e^r - 1 - t1 = rl + r^2 (1/2 + r/6) (truncation below 1e-15 for
+// |r| <= 3.5e-4), the table gives 2^(j/2048) as a pair, and sign * 2^k * 2^(n >> 11) is one
+// float multiply (exact). Relative error within 5e-11 of the exact value over the active range
+// y in [-27.7, ln 2) (long-double comparison on the test bases); only FP32 and integer
+// instructions. Lanes outside the active range compute garbage that the caller discards.
+__device__ __forceinline__ F2 prim_pair(const PrimFold* __restrict__ F, float r2h, float r2l,
+                                        const float2* __restrict__ fine) {
+  const float nah = __ldg(&F->nah), nal = __ldg(&F->nal);
+  const float ph = __fmul_rn(nah, r2h);
+  const float pe = fmaf(nah, r2h, -ph);
+  const float pl = fmaf(nah, r2l, fmaf(nal, r2h, pe));
+  const float tf = fmaf(ph, kInvLFinef, 12582912.0f);  // 1.5 * 2^23: rounds to an integer
+  const int n1 = __float_as_int(tf) - 0x4B400000;
+  const float nf = __fsub_rn(tf, 12582912.0f);
+  const float t1 = fmaf(nf, -kLh, ph);
+  const float rl = fmaf(nf, -kLm, __fadd_rn(pl, __ldg(&F->dh)));
+  const float rr = __fadd_rn(t1, rl);
+  const float pp = fmaf(__fmul_rn(rr, rr), fmaf(rr, 1.0f / 6.0f, 0.5f), rl);
+  const int n = n1 + __ldg(&F->jm);
+  const float2 T = fine[n & (kFine - 1)];
+  const float ah = __fmul_rn(T.x, t1);
+  const float al = fmaf(T.x, t1, -ah);
+  const float s = __fadd_rn(T.x, ah);  // T.x >= 1 > |ah|: s + e = T.x + ah exactly
+  const float e = __fsub_rn(ah, __fsub_rn(s, T.x));
+  const float vl = __fadd_rn(__fadd_rn(e, al), fmaf(T.x, pp, fmaf(T.y, t1, T.y)));
+  const float sc = __uint_as_float(__ldg(&F->ebase) + ((unsigned)(n >> kFineBits) << 23));
+  return {__fmul_rn(s, sc), __fmul_rn(vl, sc)};
+}
+
+// A primitive's contribution to the radial sums of the split-BF16 form: R += v, G += -expo v,
+// H += expo^2 v (so that sum(-2 a v) = 2 G and sum(-2 a^2 v) = -2 H).
+__device__ __forceinline__ void acc_prim(F2& R, F2& G, F2& H, F2 v, float nah, float nal) {
+  add_pair(R, v);
+  const F2 m = mul_pair(nah, nal, v.h, v.l);
+  add_pair(G, m);
+  add_pair(H, mul_pair(nah, nal, m.h, m.l));
 }
 
 // Collects one warp's AO values (lane = point) for ao_vgl / ao_value and writes them as row
@@ -279,8 +325,7 @@ struct Writer<Out::Planes> {
     }
     fill += 1;
   }
-  // value, gradient and (assembled in FP64) Laplacian rounded to FP32; drop: the AO's FP64 value
-  // is zero
+  // value, gradient and Laplacian (assembled in FP32); drop: the AO's FP64 value is zero
   __device__ __forceinline__ void emit_mixed(float v0, float gx, float gy, float gz, float lapf, bool drop) {
     if (valid && row_ok()) {
       __nv_bfloat16* r = o + (int64_t)(base + fill) * row_len;
@@ -307,49 +352,82 @@ struct ShellVals {
   double R;    // radial value t0
   double t1, t2, t3;  // radial gradient = g * (x, y, z)
   double Rt;   // t4 + 2 l g, the radial part of the Laplacian after Euler's identity
-  double R2, R6;  // 2 R and 6 R (split-BF16 form, shells with l = 2 and 3)
-  float Rf, t1f, t2f, t3f;  // FP32 copies for the split-BF16 form's value and gradient
+  // split-BF16 form (FP32): the same quantities, 2 R and 6 R (shells with l = 2 and 3), and
+  // whether the FP64 radial value is zero (the AO is then dropped from the derivative rows)
+  float Rf, t1f, t2f, t3f, Rtf, R2f, R6f;
+  bool rzero;
 };
 
-// Powers 0..3 of the displacement from the nucleus, FP64 and (split-BF16 form) FP32.
+// Powers 0..3 of the displacement from the nucleus: FP64 for the FP64 outputs, FP32 for the
+// split-BF16 form.
 struct Pows {
   double X[4], Y[4], Z[4];
   float Xf[4], Yf[4], Zf[4];
 };
+
+// What the split-BF16 form needs to decide, per AO, whether the FP64 polynomial
+// P = x^a (y^b z^c) is zero (the reference's zero-value test is on the FP64 value P R f): the
+// displacements, whether each is +-0, and whether the warp needs the FP64 product itself (a
+// lane with a NaN coordinate, or a displacement below 2^-340 in magnitude that could underflow
+// the product; for l <= 3 no other product of nonzero displacements is zero).
+struct PolyZero {
+  double x, y, z;
+  bool zx, zy, zz;
+  bool exact;  // warp-uniform
+};
+
+template <int e>
+__device__ __forceinline__ double dpow(double x) {
+  if constexpr (e == 0) return 1.0;
+  else if constexpr (e == 1) return x;
+  else if constexpr (e == 2) return x * x;
+  else return (x * x) * x;
+}
+
+template <int a, int b, int c>
+__device__ __forceinline__ bool poly_zero(const PolyZero& pz) {
+  if (pz.exact) return (bits_of(dpow<a>(pz.x) * (dpow<b>(pz.y) * dpow<c>(pz.z))) << 1) == 0;
+  return (a > 0 && pz.zx) || (b > 0 && pz.zy) || (c > 0 && pz.zz);
+}
 
 // Powers up to L only, formed per shell: nothing of them stays live across the shell loop
 // (registers), and a nucleus without d or f shells multiplies nothing.
 template <Out O, int L>
 __device__ __forceinline__ Pows make_pows(double x, double y, double z, float xf, float yf, float zf) {
   Pows pw;
-  pw.X[0] = pw.Y[0] = pw.Z[0] = 1.0;
-  pw.Xf[0] = pw.Yf[0] = pw.Zf[0] = 1.f;
-  if constexpr (L >= 1) {
-    pw.X[1] = x;
-    pw.Y[1] = y;
-    pw.Z[1] = z;
-    pw.Xf[1] = xf;
-    pw.Yf[1] = yf;
-    pw.Zf[1] = zf;
-  }
-  if constexpr (L >= 2) {
-    pw.X[2] = x * x;
-    pw.Y[2] = y * y;
-    pw.Z[2] = z * z;
-    if constexpr (O == Out::Planes) {
+  if constexpr (O == Out::Planes) {
+    pw.Xf[0] = pw.Yf[0] = pw.Zf[0] = 1.f;
+    if constexpr (L >= 1) {
+      pw.Xf[1] = xf;
+      pw.Yf[1] = yf;
+      pw.Zf[1] = zf;
+    }
+    if constexpr (L >= 2) {
       pw.Xf[2] = xf * xf;
       pw.Yf[2] = yf * yf;
       pw.Zf[2] = zf * zf;
     }
-  }
-  if constexpr (L >= 3) {
-    pw.X[3] = pw.X[2] * x;
-    pw.Y[3] = pw.Y[2] * y;
-    pw.Z[3] = pw.Z[2] * z;
-    if constexpr (O == Out::Planes) {
+    if constexpr (L >= 3) {
       pw.Xf[3] = pw.Xf[2] * xf;
       pw.Yf[3] = pw.Yf[2] * yf;
       pw.Zf[3] = pw.Zf[2] * zf;
+    }
+  } else {
+    pw.X[0] = pw.Y[0] = pw.Z[0] = 1.0;
+    if constexpr (L >= 1) {
+      pw.X[1] = x;
+      pw.Y[1] = y;
+      pw.Z[1] = z;
+    }
+    if constexpr (L >= 2) {
+      pw.X[2] = x * x;
+      pw.Y[2] = y * y;
+      pw.Z[2] = z * z;
+    }
+    if constexpr (L >= 3) {
+      pw.X[3] = pw.X[2] * x;
+      pw.Y[3] = pw.Y[2] * y;
+      pw.Z[3] = pw.Z[2] * z;
     }
   }
   return pw;
@@ -358,14 +436,13 @@ __device__ __forceinline__ Pows make_pows(double x, double y, double z, float xf
 // One Cartesian component x^a y^b z^c (a, b, c compile-time), assembled like the
 // reference's src/qmckl_ao_sycl.cpp:371-420 and multiplied by the AO factor.
 template <Out O, int a, int b, int c>
-__device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVals& s, double f, bool zero) {
+__device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVals& s, double f, bool zero,
+                                     const PolyZero& pz) {
   constexpr int NC = ncomp<O>();
-  const double(&X)[4] = pw.X;
-  const double(&Y)[4] = pw.Y;
-  const double(&Z)[4] = pw.Z;
   if constexpr (O == Out::Planes) {
-    // Split-BF16 form: the planes carry 24 significant bits, so the value and gradient are
-    // assembled in FP32; the Laplacian (cancellation-prone) in FP64 as in the FP64 form.
+    // Split-BF16 form: the planes carry 24 significant bits, so every component is assembled in
+    // FP32 from the radial quantities rounded to FP32 (the Laplacian's radial part Rt is formed
+    // in pair arithmetic before that rounding, so its cancellation costs no accuracy).
     const float(&Xf)[4] = pw.Xf;
     const float(&Yf)[4] = pw.Yf;
     const float(&Zf)[4] = pw.Zf;
@@ -376,22 +453,19 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
     if constexpr (b > 0) gy = fmaf((float)b * Yf[b - 1], (Xf[a] * Zf[c]) * s.Rf, gy);
     if constexpr (c > 0) gz = fmaf((float)c * Zf[c - 1], (Xf[a] * Yf[b]) * s.Rf, gz);
     float v0 = Pf * s.Rf;
-    const double yz = Y[b] * Z[c];
-    const double P = X[a] * yz;
     // l <= 3: at most one exponent e of a, b, c is 2 or more, so the polynomial's second
     // derivatives add one term e (e - 1) x^(e-2) m R, with m the other two coordinates' powers
-    // (1, x, y or z) and x^(e-2) = 1 or the coordinate itself: lap = fma(P, Rt, (e (e - 1) R) m),
-    // e (e - 1) R formed once per shell (2R, 6R), all in FP64
+    // (1, x, y or z) and x^(e-2) = 1 or the coordinate itself: lap = fma(P, Rt, (e (e - 1) R) m)
     static_assert(a + b + c <= 3, "the fixed-l path covers l <= 3");
-    double lap;
+    float lap;
     if constexpr (a > 1) {
-      lap = fma(P, s.Rt, (a == 2 ? s.R2 : s.R6) * (X[a - 2] * yz));
+      lap = fmaf(Pf, s.Rtf, (a == 2 ? s.R2f : s.R6f) * (Xf[a - 2] * yzf));
     } else if constexpr (b > 1) {
-      lap = fma(P, s.Rt, (b == 2 ? s.R2 : s.R6) * (Y[b - 2] * (X[a] * Z[c])));
+      lap = fmaf(Pf, s.Rtf, (b == 2 ? s.R2f : s.R6f) * (Yf[b - 2] * (Xf[a] * Zf[c])));
     } else if constexpr (c > 1) {
-      lap = fma(P, s.Rt, (c == 2 ? s.R2 : s.R6) * (Z[c - 2] * (X[a] * Y[b])));
+      lap = fmaf(Pf, s.Rtf, (c == 2 ? s.R2f : s.R6f) * (Zf[c - 2] * (Xf[a] * Yf[b])));
     } else {
-      lap = P * s.Rt;
+      lap = Pf * s.Rtf;
     }
     if (!is_one(f)) {
       const float ff = f64_to_f32(f);
@@ -399,15 +473,18 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
       gx *= ff;
       gy *= ff;
       gz *= ff;
-      lap *= f;
+      lap *= ff;
     }
     // the reference's MO kernel skips an AO whose FP64 value P R f is exactly zero
-    // (src/qmckl_mo_sycl.cpp:40): decided on the bits of the factors
-    const bool drop = zero || (bits_of(P) << 1) == 0 || (bits_of(s.R) << 1) == 0 || (bits_of(f) << 1) == 0;
+    // (src/qmckl_mo_sycl.cpp:40): decided on the FP64 factors' zero tests
+    const bool drop = zero || s.rzero || (bits_of(f) << 1) == 0 || poly_zero<a, b, c>(pz);
     if (zero) v0 = 0.f;
-    w.emit_mixed(v0, gx, gy, gz, f64_to_f32(lap), drop);
+    w.emit_mixed(v0, gx, gy, gz, lap, drop);
     return;
   }
+  const double(&X)[4] = pw.X;
+  const double(&Y)[4] = pw.Y;
+  const double(&Z)[4] = pw.Z;
   const double yz = Y[b] * Z[c];
   const double P = X[a] * yz;
   double v[NC];
@@ -445,36 +522,36 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
 // (src/qmckl_ao_sycl.cpp:297-305).
 template <Out O, int L>
 __device__ __forceinline__ void shell_fixed(Writer<O>& w, const Pows& pw, const ShellVals& sv_in,
-                                            const double* __restrict__ aof, int ao0, bool zero) {
+                                            const double* __restrict__ aof, int ao0, bool zero, const PolyZero& pz) {
   ShellVals s = sv_in;
   if constexpr (O == Out::Planes && L >= 2) {
-    s.R2 = s.R + s.R;  // exact
-    if constexpr (L >= 3) s.R6 = 3.0 * s.R2;
+    s.R2f = s.Rf + s.Rf;  // exact
+    if constexpr (L >= 3) s.R6f = 3.f * s.R2f;
   }
   if constexpr (L == 0) {
-    cart<O, 0, 0, 0>(w, pw, s, __ldg(aof + ao0), zero);
+    cart<O, 0, 0, 0>(w, pw, s, __ldg(aof + ao0), zero, pz);
   } else if constexpr (L == 1) {
-    cart<O, 1, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero);
-    cart<O, 0, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero);
-    cart<O, 0, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero);
+    cart<O, 1, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero, pz);
+    cart<O, 0, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero, pz);
+    cart<O, 0, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero, pz);
   } else if constexpr (L == 2) {
-    cart<O, 2, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero);
-    cart<O, 1, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero);
-    cart<O, 1, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero);
-    cart<O, 0, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero);
-    cart<O, 0, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero);
-    cart<O, 0, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero);
+    cart<O, 2, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero, pz);
+    cart<O, 1, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero, pz);
+    cart<O, 1, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero, pz);
+    cart<O, 0, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero, pz);
+    cart<O, 0, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero, pz);
+    cart<O, 0, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero, pz);
   } else {
-    cart<O, 3, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero);
-    cart<O, 2, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero);
-    cart<O, 2, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero);
-    cart<O, 1, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero);
-    cart<O, 1, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero);
-    cart<O, 1, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero);
-    cart<O, 0, 3, 0>(w, pw, s, __ldg(aof + ao0 + 6), zero);
-    cart<O, 0, 2, 1>(w, pw, s, __ldg(aof + ao0 + 7), zero);
-    cart<O, 0, 1, 2>(w, pw, s, __ldg(aof + ao0 + 8), zero);
-    cart<O, 0, 0, 3>(w, pw, s, __ldg(aof + ao0 + 9), zero);
+    cart<O, 3, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero, pz);
+    cart<O, 2, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero, pz);
+    cart<O, 2, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero, pz);
+    cart<O, 1, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero, pz);
+    cart<O, 1, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero, pz);
+    cart<O, 1, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero, pz);
+    cart<O, 0, 3, 0>(w, pw, s, __ldg(aof + ao0 + 6), zero, pz);
+    cart<O, 0, 2, 1>(w, pw, s, __ldg(aof + ao0 + 7), zero, pz);
+    cart<O, 0, 1, 2>(w, pw, s, __ldg(aof + ao0 + 8), zero, pz);
+    cart<O, 0, 0, 3>(w, pw, s, __ldg(aof + ao0 + 9), zero, pz);
   }
 }
 
@@ -523,13 +600,21 @@ __device__ __forceinline__ void shell_generic(Writer<O>& w, double x, double y, 
 }
 
 
+// A displacement that is nonzero and below 2^-340 in magnitude (biased exponent below 683): a
+// product of such powers could underflow, so the zero test of the FP64 polynomial needs the
+// product itself.
+__device__ __forceinline__ bool tiny_disp(double x) {
+  const uint64_t b = bits_of(x) << 1;
+  return b != 0 && b < (683ull << 53);
+}
+
 // One warp task: 32 points (lane = point) x one chunk of consecutive nuclei. G: the basis has
 // shells with l >= 4 (the generic path is compiled in only then, since its local arrays and
 // extra live values cost the common kernel registers).
 template <Out O, bool G, bool B, bool S, bool kSkipDead = true>
 __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, const NucleusChunk* chunk,
                                            Stage<ncomp<O>()>* st, const double* __restrict__ thi,
-                                           const double* __restrict__ tlo, const double* __restrict__ fine,
+                                           const double* __restrict__ tlo, const float2* __restrict__ fine,
                                            double* __restrict__ ebuf, int lane) {
   constexpr int NC = ncomp<O>();
   const int64_t p0 = group * 32;
@@ -576,42 +661,166 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
       }
       continue;
     }
-    float xf = 0.f, yf = 0.f, zf = 0.f, r2f = 0.f;
-    double m2r2 = 0.0;
     if constexpr (O == Out::Planes) {
-      r2f = f64_to_f32(r2);
-      m2r2 = -2.0 * r2;
-      xf = f64_to_f32(x);
-      yf = f64_to_f32(y);
-      zf = f64_to_f32(z);
-    }
-    // Shared exponentials (B): each distinct exponent of the nucleus once per lane, kept in
-    // this lane's column of the warp's buffer; the shells' primitives then read them. The
-    // FP64 outputs evaluate coef * e^(-expo r2) with the same operations as the per-primitive
-    // loop (bit-identical results).
-    bool shared_e = false;
-    if constexpr (B) {
-      if (a.ent) {
-        shared_e = true;
-        for (int u = 0; u < N.ent_num; ++u) {
-          const PrimFold* E = a.ent + N.ent_begin + u;
-          const bool act = !scr && (r2b < __ldg(&E->thr_bits));
-          if (__any_sync(kFull, act)) {
-            double e;
-            if constexpr (O == Out::Planes) e = fold_value(E, r2, r2f, fine);
-            else e = exp_neg((-__ldg(&E->na)) * r2, thi, tlo);
-            ebuf[u * 32 + lane] = keep_if(act, e);
+      // Split-BF16 form: radials in FP32 pair arithmetic (the FP64 pipe only forms r2 and its
+      // split), assembly in FP32.
+      const float xf = f64_to_f32(x), yf = f64_to_f32(y), zf = f64_to_f32(z);
+      const float r2h = f64_to_f32(r2);
+      const float r2l = f64_to_f32(r2 - f32_to_f64(r2h));  // r2h + r2l = r2 to ~2^-48
+      PolyZero pz;
+      pz.x = x;
+      pz.y = y;
+      pz.z = z;
+      pz.zx = (bits_of(x) << 1) == 0;
+      pz.zy = (bits_of(y) << 1) == 0;
+      pz.zz = (bits_of(z) << 1) == 0;
+      pz.exact = nan_warp || __any_sync(kFull, !scr && (tiny_disp(x) || tiny_disp(y) || tiny_disp(z)));
+      const bool pairs = a.fold != nullptr;  // uniform: the basis is in the folded range
+      // Shared exponentials (B): each distinct exponent of the nucleus once per lane, as a pair
+      // in this lane's column of the warp's buffer; the shells' primitives multiply it by their
+      // coefficient.
+      bool shared_e = false;
+      if constexpr (B) {
+        if (a.ent && pairs) {
+          shared_e = true;
+          float2* eb = reinterpret_cast<float2*>(ebuf);
+          for (int u = 0; u < N.ent_num; ++u) {
+            const PrimFold* E = a.ent + N.ent_begin + u;
+            const bool act = !scr && (r2b < __ldg(&E->thr_bits));
+            if (__any_sync(kFull, act)) {
+              const F2 e = prim_pair(E, r2h, r2l, fine);
+              eb[u * 32 + lane] = make_float2(act ? e.h : 0.f, act ? e.l : 0.f);
+            }
           }
         }
       }
-    }
-    for (int si = s_begin; si < s_end; ++si) {
-      const ShellEntry S = a.shells[si];
-      double t0 = 0.0, g = 0.0, h = 0.0;
-      bool folded = false;
+      for (int si = s_begin; si < s_end; ++si) {
+        const ShellEntry S = a.shells[si];
+        F2 R{0.f, 0.f}, Gs{0.f, 0.f}, Hs{0.f, 0.f};  // sum v, sum -expo v, sum expo^2 v
+        double t0 = 0.0, g = 0.0, h = 0.0;           // FP64 sums (basis outside the folded range)
+        if (pairs) {
+          if (shared_e) {
+            const float2* eb = reinterpret_cast<const float2*>(ebuf);
+            for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+              const PrimFold* F = a.fold + pi;
+              const bool act = !scr && (r2b < __ldg(&F->thr_bits));
+              if (__any_sync(kFull, act)) {
+                const float2 e = eb[__ldg(&a.prims[pi].ent) * 32 + lane];
+                F2 v = mul_pair(__ldg(&F->ch), __ldg(&F->cl), e.x, e.y);
+                if (!act) v = F2{0.f, 0.f};
+                acc_prim(R, Gs, Hs, v, __ldg(&F->nah), __ldg(&F->nal));
+              }
+            }
+          } else {
+            for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+              const PrimFold* F = a.fold + pi;
+              const bool act = !scr && (r2b < __ldg(&F->thr_bits));
+              if (__any_sync(kFull, act)) {
+                F2 v = prim_pair(F, r2h, r2l, fine);
+                if (!act) v = F2{0.f, 0.f};
+                acc_prim(R, Gs, Hs, v, __ldg(&F->nah), __ldg(&F->nal));
+              }
+            }
+          }
+        } else {
+          for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+            const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
+            if (__any_sync(kFull, act)) {
+              const double ar2 = __ldg(&a.prims[pi].expo) * r2;
+              const double e = exp_neg(ar2, thi, tlo);
+              const double v = keep_if(act, __ldg(&a.prims[pi].coef) * e);
+              t0 += v;
+              const double two_a = __ldg(&a.prims[pi].m2a) * v;
+              g += two_a;
+              h = fma(two_a, ar2, h);
+            }
+          }
+        }
+        if (nan_warp) {
+          // every primitive of a NaN lane is NaN in the reference; the outputs follow by arithmetic
+          // (the FP32 quantities become NaN, and so does the contraction)
+          if (nanr && S.prim_end > S.prim_begin) {
+            R.h = Gs.h = Hs.h = __uint_as_float(0x7FC00000u);
+            t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
+          }
+        } else if (kSkipDead) {
+          // no lane has a nonzero radial sum (every primitive screened for the warp's points: about
+          // a third of the shells a warp evaluates on the medium workload, mostly tight core
+          // shells): the shell's AOs are zero in every component, written without the assembly
+          const bool nz = pairs ? ((__float_as_uint(R.h) | __float_as_uint(R.l) | __float_as_uint(Gs.h) |
+                                    __float_as_uint(Gs.l) | __float_as_uint(Hs.h) | __float_as_uint(Hs.l)) << 1) != 0
+                                : ((bits_of(t0) | bits_of(g) | bits_of(h)) << 1) != 0;
+          if (!__any_sync(kFull, nz)) {
+            w.emit_zeros((S.l + 1) * (S.l + 2) / 2);
+            continue;
+          }
+        }
+        ShellVals sv;
+        float gf;
+        F2 rt{0.f, 0.f};
+        double Rt = 0.0;
+        if (pairs) {
+          // Rt = sum v (4 expo^2 r2 - 2 expo (3 + 2l)) = 2 ((3 + 2l) G + 2 r2 H), the
+          // cancellation-prone part of the Laplacian, in pair arithmetic before one rounding
+          sv.Rf = __fadd_rn(R.h, R.l);
+          gf = 2.f * __fadd_rn(Gs.h, Gs.l);
+          rt = mul_pair((float)(3 + 2 * S.l), 0.f, Gs.h, Gs.l);
+          const F2 rh = mul_pair(r2h, r2l, Hs.h, Hs.l);
+          add_pair(rt, F2{2.f * rh.h, 2.f * rh.l});
+          sv.Rtf = 2.f * __fadd_rn(rt.h, rt.l);
+          sv.rzero = R.h == -R.l;  // the FP64 value R.h + R.l is zero
+        } else {
+          Rt = fma(kTwoL[S.l], g, fma(-2.0, h, 3.0 * g));
+          sv.Rf = f64_to_f32(t0);
+          gf = f64_to_f32(g);
+          sv.Rtf = f64_to_f32(Rt);
+          sv.rzero = (bits_of(t0) << 1) == 0;
+        }
+        sv.t1f = gf * xf;
+        sv.t2f = gf * yf;
+        sv.t3f = gf * zf;
+        switch (S.l) {
+          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
+          default:
+            if constexpr (G) {  // the generic path assembles in FP64
+              const double g64 = pairs ? 2.0 * (f32_to_f64(Gs.h) + f32_to_f64(Gs.l)) : g;
+              sv.R = pairs ? f32_to_f64(R.h) + f32_to_f64(R.l) : t0;
+              sv.Rt = pairs ? 2.0 * (f32_to_f64(rt.h) + f32_to_f64(rt.l)) : Rt;
+              sv.t1 = g64 * x;
+              sv.t2 = g64 * y;
+              sv.t3 = g64 * z;
+              shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
+            }
+            break;
+        }
+      }
+      continue;
+    } else {
+      // Shared exponentials (B): each distinct exponent of the nucleus once per lane, kept in
+      // this lane's column of the warp's buffer; the shells' primitives then read them
+      // (coef * e^(-expo r2) with the same operations as the per-primitive loop: bit-identical
+      // results).
+      bool shared_e = false;
       if constexpr (B) {
+        if (a.ent) {
+          shared_e = true;
+          for (int u = 0; u < N.ent_num; ++u) {
+            const PrimFold* E = a.ent + N.ent_begin + u;
+            const bool act = !scr && (r2b < __ldg(&E->thr_bits));
+            if (__any_sync(kFull, act)) {
+              const double e = exp_neg((-__ldg(&E->na)) * r2, thi, tlo);
+              ebuf[u * 32 + lane] = keep_if(act, e);
+            }
+          }
+        }
+      }
+      for (int si = s_begin; si < s_end; ++si) {
+        const ShellEntry S = a.shells[si];
+        double t0 = 0.0, g = 0.0, h = 0.0;
         if (shared_e) {
-          folded = O == Out::Planes;
           for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
             const PrimEntry* P = a.prims + pi;
             const bool act = !scr && (r2b < __ldg(&P->thr_bits));
@@ -619,10 +828,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
               double v = __ldg(&P->coef) * ebuf[__ldg(&P->ent) * 32 + lane];
               v = keep_if(act, v);
               t0 += v;
-              if constexpr (O == Out::Planes) {
-                g = fma(__ldg(&P->m2a), v, g);
-                h = fma(__ldg(&P->m2a2), v, h);
-              } else if constexpr (NC == 5) {
+              if constexpr (NC == 5) {
                 const double ar2 = __ldg(&P->expo) * r2;
                 const double two_a = __ldg(&P->m2a) * v;
                 g += two_a;
@@ -630,97 +836,57 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
               }
             }
           }
-        }
-      }
-      if constexpr (O == Out::Planes) {
-        if (!shared_e && a.fold) {  // uniform: h = sum(-2 a^2 v), so that sum(-2 a v a r2) = r2 h
-          folded = true;
+        } else {
           for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
-            const PrimFold* F = a.fold + pi;
-            const bool act = !scr && (r2b < __ldg(&F->thr_bits));
+            const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
             if (__any_sync(kFull, act)) {
-              double v = fold_value(F, r2, r2f, fine);
+              const double expo = __ldg(&a.prims[pi].expo);
+              const double ar2 = expo * r2;
+              const double e = exp_neg(ar2, thi, tlo);
+              double v = __ldg(&a.prims[pi].coef) * e;
               v = keep_if(act, v);
               t0 += v;
-              g = fma(__ldg(&F->m2a), v, g);
-              h = fma(__ldg(&F->m2a2), v, h);
+              if constexpr (NC == 5) {
+                const double two_a = __ldg(&a.prims[pi].m2a) * v;
+                g += two_a;
+                h = fma(two_a, ar2, h);
+              }
             }
           }
         }
-      }
-      if (!folded && !shared_e) {
-        for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
-          const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
-          if (__any_sync(kFull, act)) {
-            const double expo = __ldg(&a.prims[pi].expo);
-            const double ar2 = expo * r2;
-            const double e = exp_neg(ar2, thi, tlo);
-            double v = __ldg(&a.prims[pi].coef) * e;
-            v = keep_if(act, v);
-            t0 += v;
-            if constexpr (NC == 5) {
-              const double two_a = __ldg(&a.prims[pi].m2a) * v;
-              g += two_a;
-              h = fma(two_a, ar2, h);
-            }
-          }
+        if (nan_warp) {
+          // every primitive of a NaN lane is NaN in the reference; the outputs follow by arithmetic
+          if (nanr && S.prim_end > S.prim_begin) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
+        } else if (kSkipDead && !__any_sync(kFull, ((bits_of(t0) | bits_of(g) | bits_of(h)) << 1) != 0)) {
+          // no lane has a nonzero radial sum: the shell's AOs are zero in every component,
+          // written without the assembly
+          w.emit_zeros((S.l + 1) * (S.l + 2) / 2);
+          continue;
         }
-      }
-      if (nan_warp) {
-        // every primitive of a NaN lane is NaN in the reference; the outputs follow by arithmetic
-        // (the split-BF16 form's FP32 copies become infinities or NaN, and the contraction NaN)
-        if (nanr && S.prim_end > S.prim_begin) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
-      } else if (kSkipDead && !__any_sync(kFull, ((bits_of(t0) | bits_of(g) | bits_of(h)) << 1) != 0)) {
-        // no lane has a nonzero radial sum (every primitive screened for the warp's points: about
-        // a third of the shells a warp evaluates on the medium workload, mostly tight core
-        // shells): the shell's AOs are zero in every component, written without the assembly
-        w.emit_zeros((S.l + 1) * (S.l + 2) / 2);
-        continue;
-      }
-      ShellVals sv;
-      sv.R = t0;
-      if constexpr (O == Out::Planes) {
-        // FP32 value/gradient inputs; the radial part of the Laplacian stays FP64:
-        // Rt = 3 g - 2 sum(-2 a v a r2) + 2 l g
-        const float gf = f64_to_f32(g);
-        sv.Rf = f64_to_f32(t0);
-        sv.t1f = gf * xf;
-        sv.t2f = gf * yf;
-        sv.t3f = gf * zf;
-        sv.t1 = sv.t2 = sv.t3 = 0.0;
-        if (folded) {
-          sv.Rt = fma(m2r2, h, kThreePlusTwoL[S.l] * g);
-        } else {
+        ShellVals sv;
+        sv.R = t0;
+        if constexpr (NC == 5) {
+          sv.t1 = g * x;
+          sv.t2 = g * y;
+          sv.t3 = g * z;
+          // a shell without primitives has a zero radial gradient in the reference, also at a NaN
+          // coordinate (where g * x would be NaN)
+          if (nan_warp && nanr && S.prim_end == S.prim_begin) sv.t1 = sv.t2 = sv.t3 = 0.0;
           const double t4 = fma(-2.0, h, 3.0 * g);
           sv.Rt = fma(kTwoL[S.l], g, t4);
+        } else {
+          sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
         }
-      } else if constexpr (NC == 5) {
-        sv.t1 = g * x;
-        sv.t2 = g * y;
-        sv.t3 = g * z;
-        // a shell without primitives has a zero radial gradient in the reference, also at a NaN
-        // coordinate (where g * x would be NaN)
-        if (nan_warp && nanr && S.prim_end == S.prim_begin) sv.t1 = sv.t2 = sv.t3 = 0.0;
-        const double t4 = fma(-2.0, h, 3.0 * g);
-        sv.Rt = fma(kTwoL[S.l], g, t4);
-      } else {
-        sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
-      }
-      switch (S.l) {
-        case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
-        case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
-        case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
-        case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr); break;
-        default:
-          if constexpr (G) {
-            if constexpr (O == Out::Planes) {  // the generic path assembles in FP64
-              sv.t1 = g * x;
-              sv.t2 = g * y;
-              sv.t3 = g * z;
-            }
-            shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
-          }
-          break;
+        const PolyZero pz{};
+        switch (S.l) {
+          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
+          default:
+            if constexpr (G) shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
+            break;
+        }
       }
     }
   }
@@ -737,7 +903,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
 template <Out O, bool G, bool B, bool S>
 __device__ __forceinline__ void ao_task(const FusedArgs& a, int64_t task, Stage<ncomp<O>()>* st,
                                         const double* __restrict__ thi, const double* __restrict__ tlo,
-                                        const double* __restrict__ fine, double* __restrict__ ebuf, int lane) {
+                                        const float2* __restrict__ fine, double* __restrict__ ebuf, int lane) {
   int64_t t0 = a.seg_task[0], g0 = a.seg_group[0];
   const NucleusChunk* c0 = a.seg_chunks[0];
   int cn = a.seg_chunk_num[0];
@@ -767,12 +933,13 @@ __host__ __device__ constexpr size_t fused_smem(int ent_cap = 0) {
 // warp's staging buffer and exponential buffer.
 template <Out O>
 struct CtaSmem {
-  double *thi, *tlo, *fine, *ebuf;
+  double *thi, *tlo, *ebuf;
+  float2* fine;
   Stage<ncomp<O>()>* st;
   __device__ __forceinline__ CtaSmem(unsigned char* raw, const ExpTable* tab, int ent_cap, int warp) {
     thi = reinterpret_cast<double*>(raw);
     tlo = thi + 32;
-    fine = thi + 64;  // split-BF16 planes only
+    fine = reinterpret_cast<float2*>(thi + 64);  // split-BF16 planes only
     load_exp_table(tab->hi, tab->lo, thi, tlo);
     if constexpr (O == Out::Planes)
       for (int i = threadIdx.x; i < kFine; i += blockDim.x) fine[i] = tab->fine[i];
@@ -1143,6 +1310,7 @@ int ao_level_count(const AoTables& t) { return (int)t.level_offsets.size(); }
 
 bool ao_shared_exponentials(const AoTables& t, bool planes) {
   if (!t.ent) return false;
+  if (planes && !t.fold) return false;  // the planes share exponentials in the folded evaluation only
   return t.ent_forced || (planes ? share_by_default<Out::Planes>() : share_by_default<Out::Vgl>());
 }
 
@@ -1363,8 +1531,9 @@ __global__ void exp_check_kernel(const double* __restrict__ x, int64_t n, const 
 
 namespace {
 // Primitive values coef * e^(-expo r2) as the split-BF16 form's AO kernel evaluates them (the
-// folded evaluation, or the FP64 form's when the tables have no folded list), zero where the
-// primitive is screened; out[i][prim_orig[k]] for packed primitive k.
+// folded FP32 pair evaluation, hi + lo as a double, or the FP64 form's when the tables have no
+// folded list), zero where the primitive is screened; out[i][prim_orig[k]] for packed
+// primitive k.
 __global__ void prim_check_kernel(const PrimFold* __restrict__ fold, const PrimEntry* __restrict__ prims,
                                   const ExpTable* __restrict__ tab, const int32_t* __restrict__ prim_orig,
                                   const double* __restrict__ r2, int64_t n, int packed, int64_t prim_num,
@@ -1376,7 +1545,11 @@ __global__ void prim_check_kernel(const PrimFold* __restrict__ fold, const PrimE
   const double r = r2[i];
   double v = 0.0;
   if (fold) {
-    if (bits_of(r) < fold[k].thr_bits) v = fold_value(fold + k, r, f64_to_f32(r), tab->fine);
+    if (bits_of(r) < fold[k].thr_bits) {
+      const float rh = f64_to_f32(r);
+      const F2 p = prim_pair(fold + k, rh, f64_to_f32(r - f32_to_f64(rh)), tab->fine);
+      v = f32_to_f64(p.h) + f32_to_f64(p.l);
+    }
   } else if (bits_of(r) < prims[k].thr_bits) {
     v = prims[k].coef * exp_neg(prims[k].expo * r, tab->hi, tab->lo);
   }

@@ -75,29 +75,32 @@ struct NucleusChunk {
 
 // 2^(j/32), j = 0..31, as hi + lo doubles (hi = the double nearest to the value): the table of
 // the AO kernel's exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989).
-// fine[j] = the double nearest to 2^(j/kFine), the table of the split-BF16 form's primitive values.
+// fine[j] = 2^(j/kFine) as an FP32 pair (x = the float nearest to the value, y = the float
+// nearest to the remainder: 48 significant bits), the table of the split-BF16 form's primitives.
 constexpr int kFineBits = 11;
 constexpr int kFine = 1 << kFineBits;
 struct ExpTable {
   double hi[32];
   double lo[32];
-  double fine[kFine];
+  float2 fine[kFine];
 };
 
 // A primitive of the packed list prepared for the split-BF16 form's radials, which evaluate
-// v = coef * e^(-expo r2) as sign * 2^k * e^y with y = ln(mant) - expo r2, where
-// |coef| = mant * 2^k, mant in [1, 2): the coefficient multiply folds into the exponential.
-struct PrimFold {          // 64 bytes
+// v = coef * e^(-expo r2) in FP32 pair arithmetic as sign * 2^k * e^y with
+// y = ln(mant) - expo r2, |coef| = mant * 2^k, mant in [1, 2): the coefficient folds into the
+// exponential. ln(mant) = jm * L + dh with L = ln 2 / kFine, so that jm joins the table index.
+// Also the distinct exponents of a nucleus (shared exponentials, coefficient 1).
+struct PrimFold {          // 48 bytes
   uint64_t thr_bits;       // PrimEntry::thr_bits, or 0 (never active) for a zero coefficient
-  double na;               // -expo
-  double lnm;              // ln(mant), in [0, ln 2)
-  double m2a;              // -2 expo
-  double m2a2;             // -2 expo^2
-  float naf, lnmf;         // FP32 copies of na and lnm (the table index estimate)
-  int32_t k;               // binary exponent of |coef|
-  uint32_t sign;           // sign of coef, in bit 31
-  uint64_t pad;
+  float nah, nal;          // -expo as an FP32 pair (nah + nal = -expo to 48 bits)
+  float dh;                // ln(mant) - jm L, |dh| <= L / 2
+  int32_t jm;              // nearest integer to ln(mant) / L, in [0, kFine]
+  uint32_t ebase;          // (k + 127) << 23 | sign of coef in bit 31: sign * 2^k as a float
+  float ch, cl;            // coef as an FP32 pair (shared exponentials: v = coef * e)
+  int32_t pad;
+  double na;               // -expo (the FP64 outputs' shared exponentials)
 };
+static_assert(sizeof(PrimFold) == 48, "PrimFold is 48 bytes");
 
 struct AoTables {
   NucleusEntry* nuclei = nullptr;   // [nucl_num]
@@ -117,7 +120,7 @@ struct AoTables {
   // the forward AO kernel's last segment).
   int32_t piece_offset = 0, piece_num = 0;
   ExpTable* exp_table = nullptr;    // device copy of the exponential's table
-  // [prim_num] packed, or null when some exponent or coefficient is outside the folded
+  // [prim_num] packed, or null when some exponent or coefficient is outside the FP32 folded
   // evaluation's range (then the split-BF16 form evaluates its radials like the FP64 form)
   PrimFold* fold = nullptr;
   // Distinct exponents per nucleus (NucleusEntry::ent_begin/ent_num), as PrimFold entries with
