@@ -61,16 +61,20 @@ uint64_t prim_threshold(double expo) {
 
 // The split-BF16 form's record of one primitive (or, with coef 1, one distinct exponent):
 // -expo as an FP32 pair, |coef| = mant 2^k with ln(mant) = jm L + dh (L = ln 2 / kFine, jm the
-// nearest integer), sign * 2^k as float bits, coef as an FP32 pair. The remainders are formed
-// in long double, then rounded once to float.
-PrimFold fold_entry(double expo, double coef, uint64_t thr_bits) {
+// nearest integer), sign * 2^k as float bits packed with jm, and coef as an FP32 pair (a
+// distinct exponent keeps -expo as a double there instead). The remainders are formed in long
+// double, then rounded once to float.
+PrimFold fold_entry(double expo, double coef, uint64_t thr_bits, bool distinct_exponent) {
   PrimFold f{};
   f.thr_bits = thr_bits;
-  f.na = -expo;
   f.nah = (float)(-expo);
   f.nal = (float)(-expo - (double)f.nah);  // the difference is exact in double
-  f.ch = (float)coef;
-  f.cl = (float)(coef - (double)f.ch);
+  if (distinct_exponent) {
+    f.na = -expo;
+  } else {
+    f.c.ch = (float)coef;
+    f.c.cl = (float)(coef - (double)f.c.ch);
+  }
   if (coef != 0.0 && std::isfinite(coef)) {
     int e2 = 0;
     const double m = std::frexp(std::fabs(coef), &e2);  // |coef| = m 2^e2, m in [0.5, 1)
@@ -78,9 +82,10 @@ PrimFold fold_entry(double expo, double coef, uint64_t thr_bits) {
     const long double L = logl(2.0L) / (long double)kFine;
     const long double lnm = logl(2.0L * (long double)m);
     const long double jm = roundl(lnm / L);
-    f.jm = (int32_t)jm;
     f.dh = (float)(lnm - jm * L);
-    f.ebase = ((uint32_t)(std::min(std::max(k, -126), 127) + 127) << 23) | (std::signbit(coef) ? 0x80000000u : 0u);
+    const uint32_t ebase =
+        ((uint32_t)(std::min(std::max(k, -126), 127) + 127) << 23) | (std::signbit(coef) ? 0x80000000u : 0u);
+    f.jeb = ebase | ((uint32_t)jm & kFoldJmMask);
   }
   return f;
 }
@@ -362,7 +367,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
   for (size_t i = 0; i < t.h_prims.size(); ++i) {
     const PrimEntry& pe = t.h_prims[i];
     if (!(pe.expo >= 0x1p-60) || !(pe.expo <= 0x1p60) || !std::isfinite(pe.coef)) fold_ok = false;
-    t.h_fold[i] = fold_entry(pe.expo, pe.coef, pe.coef == 0.0 ? 0 : pe.thr_bits);
+    t.h_fold[i] = fold_entry(pe.expo, pe.coef, pe.coef == 0.0 ? 0 : pe.thr_bits, false);
     if (pe.coef != 0.0 && std::isfinite(pe.coef)) {
       int e2 = 0;
       std::frexp(pe.coef, &e2);
@@ -422,7 +427,7 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
       for (int32_t p = p0; p < p1; ++p) w_all += std::pow(t.h_prims[(size_t)p].expo, -1.5);
       for (double a : ex) {
         w_ent += std::pow(a, -1.5);
-        t.h_ent.push_back(fold_entry(a, 1.0, prim_threshold(a)));
+        t.h_ent.push_back(fold_entry(a, 1.0, prim_threshold(a), true));
       }
       for (int32_t p = p0; p < p1; ++p)
         t.h_prims[(size_t)p].ent =

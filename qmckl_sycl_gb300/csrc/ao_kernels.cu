@@ -36,8 +36,12 @@
 //    0 and 1 fold away); higher l takes a generic path;
 //  * results are staged per warp in shared memory and stored as contiguous row
 //    segments, so global stores are coalesced whatever the point order.
+// The split-BF16 form's planes carry 24 significant bits, so its kernel keeps the FP64 pipe for
+// r2 alone (the screening inputs): primitives, radial sums and the radial Laplacian factor run in
+// FP32 pair arithmetic (~44 bits), the per-AO assembly in FP32.
 #include <cuda_bf16.h>
 
+#include <cstddef>
 #include <cstdint>
 
 #include "internal.hpp"
@@ -58,6 +62,11 @@ constexpr int kTasksPerWarp = QMCKL_AO_TASKS_PER_WARP;
 // Segments of a launch's schedule (1: every task at the chosen level; more: the last point
 // groups at finer levels, down to pieces of nuclei).
 constexpr int kTailSegments = QMCKL_AO_TAIL_SEGMENTS;
+#ifndef QMCKL_AO_BATCH_PLANES_SKIP_DEAD
+#define QMCKL_AO_BATCH_PLANES_SKIP_DEAD 0
+#endif
+// Whether the batch kernel's planes skip the assembly of shells that are zero on every lane.
+constexpr bool kBatchPlanesSkipDead = QMCKL_AO_BATCH_PLANES_SKIP_DEAD != 0;
 using namespace dev;
 
 enum class Out { Vgl, Value, Planes };
@@ -66,12 +75,17 @@ __host__ __device__ constexpr int ncomp() {
   return O == Out::Value ? 1 : 5;
 }
 // Resident CTAs per SM the register allocation must allow. The planes output stages nothing in
-// shared memory, so registers alone bound its occupancy: 6 CTAs (24 warps) per SM measured
-// 2.13 ms against 2.76 ms with the compiler's unconstrained allocation (4 CTAs) on the medium
-// workload. The staged ao_vgl output fits 5 CTAs in shared memory, ao_value 8 or more.
+// shared memory, so registers alone bound its occupancy: 7 CTAs (28 warps, 72 registers) per SM
+// measured 0.559 ms against 0.586 / 0.575 ms with 6 / 8 on the medium workload (the FP32 pair
+// radials; with the earlier FP64 radials 6 CTAs measured 2.13 ms against 2.76 ms with the
+// compiler's unconstrained 4). The staged ao_vgl output fits 5 CTAs in shared memory, ao_value 8
+// or more.
+#ifndef QMCKL_AO_PLANES_CTAS
+#define QMCKL_AO_PLANES_CTAS 7
+#endif
 template <Out O>
 __host__ __device__ constexpr int min_ctas() {
-  return O == Out::Planes ? 6 : (O == Out::Vgl ? 5 : 8);
+  return O == Out::Planes ? QMCKL_AO_PLANES_CTAS : (O == Out::Vgl ? 5 : 8);
 }
 
 // Dynamic shared memory: the exponential's tables (2 x 32 doubles, plus the split-BF16 form's
@@ -160,18 +174,42 @@ constexpr double kLFine = 0.6931471805599453094 / kFine;              // ln 2 / 
 constexpr float kLh = (float)kLFine;                                   // as an FP32 pair
 constexpr float kLm = (float)(kLFine - (double)kLh);
 
+// A PrimFold loaded as two 16-byte vectors instead of one load per field.
+struct FoldRec {
+  uint64_t thr;
+  float nah, nal, dh;
+  uint32_t jeb;
+  float ch, cl;
+};
+static_assert(offsetof(PrimFold, nah) == 8 && offsetof(PrimFold, dh) == 16 && offsetof(PrimFold, jeb) == 20 &&
+                  offsetof(PrimFold, c) == 24,
+              "FoldRec reads PrimFold's fields in this order");
+__device__ __forceinline__ FoldRec load_fold(const PrimFold* __restrict__ F) {
+  const uint4 q0 = __ldg(reinterpret_cast<const uint4*>(F));
+  const uint4 q1 = __ldg(reinterpret_cast<const uint4*>(F) + 1);
+  FoldRec r;
+  r.thr = (uint64_t)q0.x | ((uint64_t)q0.y << 32);
+  r.nah = __uint_as_float(q0.z);
+  r.nal = __uint_as_float(q0.w);
+  r.dh = __uint_as_float(q1.x);
+  r.jeb = q1.y;
+  r.ch = __uint_as_float(q1.z);
+  r.cl = __uint_as_float(q1.w);
+  return r;
+}
+
 // One primitive of the split-BF16 form, v = coef * e^(-expo r2), as an FP32 pair, for
-// r2 = r2h + r2l (an FP32 pair). With y = -expo r2 + ln(mant) and n = n1 + jm:
-//   e^y = 2^(n >> 11) * 2^((n & 2047)/2048) * e^r,  r = (p - n1 L) + (dh + low parts),
-// where p = fl(-expo r2h) and n1 = round(p / L). t1 = p - n1 Lh is exact (|t1| < 2^-12 and both
-// terms are multiples of 2^-35), e^r - 1 - t1 = rl + r^2 (1/2 + r/6) (truncation below 1e-15 for
-// |r| <= 3.5e-4), the table gives 2^(j/2048) as a pair, and sign * 2^k * 2^(n >> 11) is one
-// float multiply (exact). Relative error within 5e-11 of the exact value over the active range
-// y in [-27.7, ln 2) (long-double comparison on the test bases); only FP32 and integer
-// instructions. Lanes outside the active range compute garbage that the caller discards.
-__device__ __forceinline__ F2 prim_pair(const PrimFold* __restrict__ F, float r2h, float r2l,
-                                        const float2* __restrict__ fine) {
-  const float nah = __ldg(&F->nah), nal = __ldg(&F->nal);
+// r2 = r2h + r2l (an FP32 pair). With L = ln 2 / 1024, y = -expo r2 + ln(mant) and n = n1 + jm:
+//   e^y = 2^(n >> 10) * 2^((n & 1023)/1024) * e^r,  r = (p - n1 L) + (dh + low parts),
+// where p = fl(-expo r2h) and n1 = round(p / L). t1 = p - n1 Lh is exact (|t1| < 2^-11 and both
+// terms are multiples of 2^-34, or of 2^-35 when |p| < 2^-11), e^r - 1 - t1 = rl + r^2 (1/2 + r/6)
+// (truncation below 1e-14 for |r| <= 7e-4), the table gives 2^(j/1024) as a pair, and
+// sign * 2^k * 2^(n >> 10) is one float multiply (exact). Relative error within 1e-10 of the
+// exact value over the active range y in [-27.7, ln 2) (long-double comparison on the test
+// bases; the rounding of rl, |rl| <= L / 2, dominates); only FP32 and integer instructions. Lanes
+// outside the active range compute garbage that the caller discards.
+__device__ __forceinline__ F2 prim_pair(const FoldRec& F, float r2h, float r2l, const float2* __restrict__ fine) {
+  const float nah = F.nah, nal = F.nal;
   const float ph = __fmul_rn(nah, r2h);
   const float pe = fmaf(nah, r2h, -ph);
   const float pl = fmaf(nah, r2l, fmaf(nal, r2h, pe));
@@ -179,17 +217,17 @@ __device__ __forceinline__ F2 prim_pair(const PrimFold* __restrict__ F, float r2
   const int n1 = __float_as_int(tf) - 0x4B400000;
   const float nf = __fsub_rn(tf, 12582912.0f);
   const float t1 = fmaf(nf, -kLh, ph);
-  const float rl = fmaf(nf, -kLm, __fadd_rn(pl, __ldg(&F->dh)));
+  const float rl = fmaf(nf, -kLm, __fadd_rn(pl, F.dh));
   const float rr = __fadd_rn(t1, rl);
   const float pp = fmaf(__fmul_rn(rr, rr), fmaf(rr, 1.0f / 6.0f, 0.5f), rl);
-  const int n = n1 + __ldg(&F->jm);
+  const int n = n1 + (int)(F.jeb & kFoldJmMask);
   const float2 T = fine[n & (kFine - 1)];
   const float ah = __fmul_rn(T.x, t1);
   const float al = fmaf(T.x, t1, -ah);
   const float s = __fadd_rn(T.x, ah);  // T.x >= 1 > |ah|: s + e = T.x + ah exactly
   const float e = __fsub_rn(ah, __fsub_rn(s, T.x));
   const float vl = __fadd_rn(__fadd_rn(e, al), fmaf(T.x, pp, fmaf(T.y, t1, T.y)));
-  const float sc = __uint_as_float(__ldg(&F->ebase) + ((unsigned)(n >> kFineBits) << 23));
+  const float sc = __uint_as_float((F.jeb & ~kFoldJmMask) + ((unsigned)(n >> kFineBits) << 23));
   return {__fmul_rn(s, sc), __fmul_rn(vl, sc)};
 }
 
@@ -685,8 +723,8 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
           shared_e = true;
           float2* eb = reinterpret_cast<float2*>(ebuf);
           for (int u = 0; u < N.ent_num; ++u) {
-            const PrimFold* E = a.ent + N.ent_begin + u;
-            const bool act = !scr && (r2b < __ldg(&E->thr_bits));
+            const FoldRec E = load_fold(a.ent + N.ent_begin + u);
+            const bool act = !scr && (r2b < E.thr);
             if (__any_sync(kFull, act)) {
               const F2 e = prim_pair(E, r2h, r2l, fine);
               eb[u * 32 + lane] = make_float2(act ? e.h : 0.f, act ? e.l : 0.f);
@@ -702,23 +740,23 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
           if (shared_e) {
             const float2* eb = reinterpret_cast<const float2*>(ebuf);
             for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
-              const PrimFold* F = a.fold + pi;
-              const bool act = !scr && (r2b < __ldg(&F->thr_bits));
+              const FoldRec F = load_fold(a.fold + pi);
+              const bool act = !scr && (r2b < F.thr);
               if (__any_sync(kFull, act)) {
                 const float2 e = eb[__ldg(&a.prims[pi].ent) * 32 + lane];
-                F2 v = mul_pair(__ldg(&F->ch), __ldg(&F->cl), e.x, e.y);
+                F2 v = mul_pair(F.ch, F.cl, e.x, e.y);
                 if (!act) v = F2{0.f, 0.f};
-                acc_prim(R, Gs, Hs, v, __ldg(&F->nah), __ldg(&F->nal));
+                acc_prim(R, Gs, Hs, v, F.nah, F.nal);
               }
             }
           } else {
             for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
-              const PrimFold* F = a.fold + pi;
-              const bool act = !scr && (r2b < __ldg(&F->thr_bits));
+              const FoldRec F = load_fold(a.fold + pi);
+              const bool act = !scr && (r2b < F.thr);
               if (__any_sync(kFull, act)) {
                 F2 v = prim_pair(F, r2h, r2l, fine);
                 if (!act) v = F2{0.f, 0.f};
-                acc_prim(R, Gs, Hs, v, __ldg(&F->nah), __ldg(&F->nal));
+                acc_prim(R, Gs, Hs, v, F.nah, F.nal);
               }
             }
           }
@@ -1004,7 +1042,8 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
     // the FP64 outputs skip shells that are zero on every lane (64-molecule ao_vgl 6.06 -> 5.33 ms);
     // the planes do not: there the test cost the batch kernel more than it saved (2.26 ms without,
     // 2.38 ms with it, also with the arguments copied to shared memory)
-    ao_task_at<O, G, B, false, O != Out::Planes>(a, g, a.chunks + (local - g * cn), sm.st, sm.thi, sm.tlo, sm.fine,
+    ao_task_at<O, G, B, false, O != Out::Planes || kBatchPlanesSkipDead>(a, g, a.chunks + (local - g * cn), sm.st,
+                                                                          sm.thi, sm.tlo, sm.fine,
                                                  sm.ebuf, lane);
   }
 }
@@ -1547,7 +1586,7 @@ __global__ void prim_check_kernel(const PrimFold* __restrict__ fold, const PrimE
   if (fold) {
     if (bits_of(r) < fold[k].thr_bits) {
       const float rh = f64_to_f32(r);
-      const F2 p = prim_pair(fold + k, rh, f64_to_f32(r - f32_to_f64(rh)), tab->fine);
+      const F2 p = prim_pair(load_fold(fold + k), rh, f64_to_f32(r - f32_to_f64(rh)), tab->fine);
       v = f32_to_f64(p.h) + f32_to_f64(p.l);
     }
   } else if (bits_of(r) < prims[k].thr_bits) {

@@ -77,7 +77,7 @@ struct NucleusChunk {
 // the AO kernel's exponential (table-driven method of P. T. P. Tang, ACM TOMS 15(2), 1989).
 // fine[j] = 2^(j/kFine) as an FP32 pair (x = the float nearest to the value, y = the float
 // nearest to the remainder: 48 significant bits), the table of the split-BF16 form's primitives.
-constexpr int kFineBits = 11;
+constexpr int kFineBits = 10;
 constexpr int kFine = 1 << kFineBits;
 struct ExpTable {
   double hi[32];
@@ -89,18 +89,24 @@ struct ExpTable {
 // v = coef * e^(-expo r2) in FP32 pair arithmetic as sign * 2^k * e^y with
 // y = ln(mant) - expo r2, |coef| = mant * 2^k, mant in [1, 2): the coefficient folds into the
 // exponential. ln(mant) = jm * L + dh with L = ln 2 / kFine, so that jm joins the table index.
-// Also the distinct exponents of a nucleus (shared exponentials, coefficient 1).
-struct PrimFold {          // 48 bytes
+// Also the distinct exponents of a nucleus (shared exponentials, coefficient 1). 32 bytes, so
+// that the medium basis's list (2123 primitives, 68 KB) stays in L1 beside the other tables.
+struct PrimFold {
   uint64_t thr_bits;       // PrimEntry::thr_bits, or 0 (never active) for a zero coefficient
   float nah, nal;          // -expo as an FP32 pair (nah + nal = -expo to 48 bits)
   float dh;                // ln(mant) - jm L, |dh| <= L / 2
-  int32_t jm;              // nearest integer to ln(mant) / L, in [0, kFine]
-  uint32_t ebase;          // (k + 127) << 23 | sign of coef in bit 31: sign * 2^k as a float
-  float ch, cl;            // coef as an FP32 pair (shared exponentials: v = coef * e)
-  int32_t pad;
-  double na;               // -expo (the FP64 outputs' shared exponentials)
+  uint32_t jeb;            // jm (nearest integer to ln(mant) / L, in [0, kFine]) in bits 0..11,
+                           // sign * 2^k as float bits (sign, biased exponent) in bits 23..31
+  union {
+    struct {
+      float ch, cl;        // a primitive: coef as an FP32 pair (shared exponentials: v = coef * e)
+    } c;
+    double na;             // a distinct exponent: -expo (the FP64 outputs' shared exponentials)
+  };
 };
-static_assert(sizeof(PrimFold) == 48, "PrimFold is 48 bytes");
+static_assert(sizeof(PrimFold) == 32, "PrimFold is 32 bytes");
+constexpr uint32_t kFoldJmMask = 0xFFFu;
+
 
 struct AoTables {
   NucleusEntry* nuclei = nullptr;   // [nucl_num]

@@ -383,10 +383,10 @@ def test_split_form_primitive_values(name, chbrclf):
     assert np.array_equal(got == 0.0, want == 0.0)
     ok = np.abs(want) > 1e-290  # normal results
     rel = (np.abs(got[ok] - exact[ok]) / np.abs(exact[ok])).astype(np.float64)
-    # folded evaluation in FP32 pair arithmetic (~44 significant bits): within 1e-10 relative; the
+    # folded evaluation in FP32 pair arithmetic (~44 significant bits): within 2e-10 relative; the
     # FP64 form's evaluation (a coefficient outside the folded range): the argument's rounding
     # (|expo r2| ulp / 2) plus a few units of 1e-16
-    bound = 1.2e-16 * ar2[ok] + 6e-16 if name == "extreme_coefficient" else np.full(rel.shape, 1e-10)
+    bound = 1.2e-16 * ar2[ok] + 6e-16 if name == "extreme_coefficient" else np.full(rel.shape, 2e-10)
     print("%s: max rel err %.2e, max err / bound %.2f" % (name, rel.max(), (rel / bound).max()))
     assert (rel <= bound).all()
 
