@@ -305,29 +305,31 @@ struct Writer {
   }
 };
 
-// The split-BF16 form's AO operand, written M-major straight from registers: plane p, AO k,
-// operand row c * pp + s (component c of the point at processing slot s) at
-// planes[(p * kp + k) * 5 pp + c * pp + s]. The 32 lanes of a warp hold 32 consecutive slots,
-// so every store of the warp fills 64 contiguous bytes (two whole sectors) and nothing is
-// staged in shared memory. Slots past the last point (padding rows) are not written; the
-// contraction discards their rows.
+// The split-BF16 form's AO operand, written straight from registers. Each plane is an M-major
+// matrix [kp][5 pp] whose operand row (5 g + c) 64 + j is component c of the point at processing
+// slot 64 g + j (64-point blocks, pp a multiple of 64): plane p, AO k of that point and component
+// at planes[(p kp + k) 5 pp + (5 g + c) 64 + j]. A lane's five components of one AO then lie at
+// fixed offsets (64 elements apart) from one address per plane, instead of pp apart (one address
+// computation per store), and the 32 lanes of a warp (32 consecutive slots, half a block) fill 64
+// contiguous bytes per store (two whole sectors); nothing is staged in shared memory. Slots past
+// the last point (padding rows) are not written; the contraction discards their rows.
 template <>
 struct Writer<Out::Planes> {
   static constexpr int NC = 5;
-  __nv_bfloat16* o;          // plane 0, AO row 0, this lane's processing slot
-  int64_t plane_stride;      // kp * 5 pp
-  int64_t row_len;           // 5 pp (elements per AO row)
-  int32_t pp;
+  static constexpr int kBlock = 64;  // points per block (and elements between components)
+  __nv_bfloat16* o;          // this lane's element of plane 0, component 0, AO row 0
+  int64_t row_len;           // elements between consecutive AOs: 5 pp
+  int64_t plane_stride;      // elements between the planes: kp 5 pp
   int base;                  // AO index of the next emit
   int fill;
   bool valid;                // the lane holds a point
-  int64_t slot;              // p0 + lane: offset of o in the planes (bounds-checked build)
+  int64_t slot;              // offset of o in the planes (bounds-checked build)
 
   __device__ __forceinline__ void init(const FusedArgs& a, Stage<5>*, int64_t p0, int ln, int nv, int64_t,
                                        int ao_begin) {
-    o = static_cast<__nv_bfloat16*>(a.planes) + p0 + ln;
-    slot = p0 + ln;
-    pp = (int32_t)a.plane_pp;
+    // p0 is a multiple of 32: block p0 / 64, half (p0 / 32) % 2
+    slot = (p0 / kBlock) * (5 * kBlock) + (p0 & (kBlock - 1)) + ln;
+    o = static_cast<__nv_bfloat16*>(a.planes) + slot;
     row_len = 5 * a.plane_pp;
     plane_stride = a.row_len * 5 * a.plane_pp;
     base = ao_begin;
@@ -343,7 +345,7 @@ struct Writer<Out::Planes> {
   __device__ __forceinline__ bool row_ok() const {
     const int64_t first = slot + (int64_t)(base + fill) * row_len;
     return QG_STORE_OK(kSiteAoPlanes, first, 3 * plane_stride) &&
-           QG_STORE_OK(kSiteAoPlanes, first + 2 * plane_stride + 4 * pp, 3 * plane_stride);
+           QG_STORE_OK(kSiteAoPlanes, first + 2 * plane_stride + 4 * kBlock, 3 * plane_stride);
   }
   __device__ __forceinline__ void emit(const double (&v)[NC]) {
     if (valid && row_ok()) {
@@ -356,9 +358,9 @@ struct Writer<Out::Planes> {
       for (int c = 0; c < NC; ++c) {
         __nv_bfloat16 h, m, l;
         split_bf16x3(c > 0 && drop ? 0.0 : v[c], h, m, l);
-        r[c * pp] = h;
-        r[plane_stride + c * pp] = m;
-        r[2 * plane_stride + c * pp] = l;
+        r[c * kBlock] = h;
+        r[plane_stride + c * kBlock] = m;
+        r[2 * plane_stride + c * kBlock] = l;
       }
     }
     fill += 1;
@@ -372,9 +374,9 @@ struct Writer<Out::Planes> {
       for (int c = 0; c < NC; ++c) {
         __nv_bfloat16 h, m, l;
         split_bf16x3f(vals[c], h, m, l);
-        r[c * pp] = h;
-        r[plane_stride + c * pp] = m;
-        r[2 * plane_stride + c * pp] = l;
+        r[c * kBlock] = h;
+        r[plane_stride + c * kBlock] = m;
+        r[2 * plane_stride + c * kBlock] = l;
       }
     }
     fill += 1;
@@ -1377,7 +1379,7 @@ FusedArgs make_fused_args(const AoTables& t, int level, const double* coord, con
   a.point_num = point_num;
   a.ao_num = t.ao_num;
   a.row_len = row_len;
-  a.plane_pp = (point_num + 31) / 32 * 32;
+  a.plane_pp = (point_num + 63) / 64 * 64;
   a.coord_ld = point_num;
   a.task_num = ((point_num + 31) / 32) * a.chunk_num;
   a.nseg = 1;

@@ -189,7 +189,7 @@ qmckl_exit_code_device prepare_members(Batch* b, std::vector<Member>& out) {
       e.kp = split_k_pad(e.A);
       rc = split_prepare_coef(m, h, e.kp);
       if (rc != QMCKL_SUCCESS_DEVICE) return fail(lead, rc, fn, "coefficient planes");
-      e.planes = split_a_planes(m, 5 * ((e.P + 31) / 32 * 32), e.kp);
+      e.planes = split_a_planes(m, 5 * ((e.P + 63) / 64 * 64), e.kp);
       if (!e.planes) return fail(lead, QMCKL_ALLOCATION_FAILED_DEVICE, fn, "AO planes");
     } else {
       if (!ensure(m, &ao.ao_vgl, &ao.ao_vgl_cap, sizeof(double) * 5 * e.A * e.P))
@@ -288,7 +288,7 @@ qmckl_exit_code_device build_descriptors(Batch* b, const std::vector<Member>& ms
     const int n_cap = b->tune.v[2] < 0 ? 160 : b->tune.v[2];
     for (int i = 0; i < n; ++i) {
       const Member& e = ms[g_order[i]];
-      const int t = split_make_job_mn(split_jobs.data() + jb * i, e.planes, (e.P + 31) / 32 * 32, e.P,
+      const int t = split_make_job_mn(split_jobs.data() + jb * i, e.planes, (e.P + 63) / 64 * 64, e.P,
                                       e.ctx->ao_basis.point_perm, e.ctx->mo_basis.coef_split, e.M, e.kp, e.mo_vgl,
                                       (int)tiles, n_cap);
       if (t < 0) return fail(lead, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");

@@ -442,11 +442,13 @@ struct FusedArgs {
   const double* coord;      // [3][coord_ld]: x of point p at coord[p], y at coord[coord_ld + p], ...
   const int32_t* perm;      // processing order of the points, or null
   double* out;              // ao_vgl (FP64 output)
-  void* planes;             // BF16 planes [3][row_len][5 plane_pp], M-major (split-BF16 output)
+  void* planes;             // BF16 planes of the split-BF16 output [3][row_len][5 plane_pp], M-major,
+                            // rows in 64-point blocks: row (5 g + c) 64 + j = component c of slot
+                            // 64 g + j
   int64_t point_num;
   int64_t ao_num;
   int64_t row_len;          // ao_num, or the padded K of the planes
-  int64_t plane_pp;         // points rounded up to a multiple of 32
+  int64_t plane_pp;         // points rounded up to a multiple of 64
   int64_t coord_ld;         // row stride of coord (point_num, or more for a slice of a larger set)
   int64_t task_num;
   int chunk_num;

@@ -290,10 +290,11 @@ struct alignas(64) SplitJob {
   int32_t n_tile;     // columns per tile (multiple of 16, <= kMaxN)
   int32_t col_tiles;  // tiles along the columns
   int32_t tile_begin; // index of this job's first tile in the launch
-  // M-major A (the fused AO kernel's plane layout): operand row r = c * pp + s is component c
-  // of the point at processing slot s; it lands in output row 5 * perm[s] + c (s < npts).
+  // M-major A (the fused AO kernel's 64-point blocks): operand row r = (5 g + c) 64 + j is
+  // component c of the point at processing slot s = 64 g + j; it lands in output row
+  // 5 * perm[s] + c (s < npts).
   int32_t a_mn;
-  int32_t pp;         // points padded to a multiple of 32 (rows = 5 pp)
+  int32_t pp;         // points padded to a multiple of 64 (rows = 5 pp)
   int64_t npts;
   const int32_t* perm;  // processing order (null: identity)
 };
@@ -455,7 +456,7 @@ __device__ __forceinline__ bool fold_tile(const FoldCtx& f, const SplitJob& job,
   const int64_t row = (int64_t)tr.m0 + f.quarter * 32 + f.lane;
   int64_t orow = row < job.rows ? row : -1;
   if (job.a_mn && orow >= 0) {
-    const int64_t comp = orow / job.pp, slot = orow - comp * job.pp;
+    const int64_t q = orow / 64, g = q / 5, comp = q - 5 * g, slot = 64 * g + (orow - 64 * q);
     orow = slot < job.npts ? 5 * (job.perm ? (int64_t)job.perm[slot] : slot) + comp : -1;
   }
   const int groups = (job.kblocks + kFold - 1) / kFold;
@@ -838,11 +839,13 @@ int make_job(SplitJob& job, const __nv_bfloat16* ap, int64_t rows, const __nv_bf
   return (int)((rows + kBM - 1) / kBM) * job.col_tiles;
 }
 
-// The mo_vgl contraction from the fused AO kernel's M-major planes ap ([3][kp][5 pp], row
-// c * pp + s = component c of processing slot s) into out[5 npts][M] (rows 5 perm[s] + c).
+// The mo_vgl contraction from the fused AO kernel's M-major planes ap ([3][kp][5 pp], pp a
+// multiple of 64; operand row (5 g + c) 64 + j = component c of processing slot 64 g + j) into
+// out[5 npts][M] (rows 5 perm[s] + c).
 int make_job_mn(SplitJob& job, const __nv_bfloat16* ap, int64_t pp, int64_t npts, const int32_t* perm,
                 const __nv_bfloat16* bp, int64_t M, int64_t kp, double* out, int tile_begin, int n_cap = kMaxN) {
   memset(&job, 0, sizeof job);
+  if (pp % 64 != 0) return -1;
   const int n_tile = tile_cols(M, n_cap);
   const int64_t rows = 5 * pp;
   for (int i = 0; i < 3; ++i)
@@ -987,7 +990,7 @@ static qmckl_exit_code_device split_mo_vgl(Ctx* ctx, qmckl_context_device c, dou
   const char* fn = "qmckl_provide_mo_basis_mo_vgl_device";
   const int64_t P = ctx->point.num, A = ctx->ao_basis.ao_num, M = ctx->mo_basis.mo_num;
   if (P <= 0 || M <= 0) return QMCKL_SUCCESS_DEVICE;
-  const int64_t pp = round_up(P, 32), rows = 5 * pp, kp = round_up(A, kBK);
+  const int64_t pp = round_up(P, 64), rows = 5 * pp, kp = round_up(A, kBK);
   if (rows > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
   qmckl_exit_code_device rc = ensure_tables(ctx, c);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -1033,22 +1036,22 @@ void* split_a_planes(Ctx* ctx, int64_t rows, int64_t kp) {
 }
 
 // Point ranges of the host-buffer path: sizes in the ratio 1 : ratio : ratio^2 ... (ratio 1: equal
-// ranges), multiples of 32 points, the last range taking the rest.
+// ranges), multiples of 64 points (the AO planes' block), the last range taking the rest.
 // Ranges sized by the contraction's waves: each range but the last has the most points (a
-// multiple of 32) whose tiles fill `waves` waves of one tile per SM, with waves = 1 unless that
+// multiple of 64) whose tiles fill `waves` waves of one tile per SM, with waves = 1 unless that
 // needs more than max_ranges ranges; the last range takes the rest. A range whose tiles end a
 // wave exactly leaves no SM idle at its end: on the medium workload (M = 300, two column tiles
 // of 150) ranges of 1920 points, 150 tiles each.
 std::vector<int64_t> wave_plan(int64_t P, int64_t M, int sms, int max_ranges) {
   const int64_t col_tiles = (M + tile_cols(M) - 1) / tile_cols(M);
-  int64_t n = 32;
+  int64_t n = 64;
   for (int64_t waves = 1;; ++waves) {
     const int64_t row_tiles = waves * sms / col_tiles;  // rows 5 n <= row_tiles * kBM
-    n = row_tiles * kBM / 5 / 32 * 32;
-    if (n >= 32 && (P + n - 1) / n <= max_ranges) break;
+    n = row_tiles * kBM / 5 / 64 * 64;
+    if (n >= 64 && (P + n - 1) / n <= max_ranges) break;
     if (row_tiles * kBM / 5 >= P) break;
   }
-  if (n < 32) n = 32;
+  if (n < 64) n = 64;
   std::vector<int64_t> sizes;
   for (int64_t done = 0; done < P; done += n) sizes.push_back(n < P - done ? n : P - done);
   return sizes;
@@ -1061,8 +1064,8 @@ std::vector<int64_t> chunk_plan(int64_t P, int chunks, double ratio) {
   int64_t done = 0;
   w = 1.0;
   for (int k = 0; k < chunks && done < P; ++k, w *= ratio) {
-    int64_t n = k == chunks - 1 ? P - done : round_up((int64_t)(P * (w / total)), 32);
-    if (n < 32) n = 32;
+    int64_t n = k == chunks - 1 ? P - done : round_up((int64_t)(P * (w / total)), 64);
+    if (n < 64) n = 64;
     if (n > P - done) n = P - done;
     sizes.push_back(n);
     done += n;
@@ -1097,8 +1100,8 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
   const int nc = (int)sizes.size();
   int64_t pc = 0;  // points of the largest range
   for (int64_t n : sizes) pc = n > pc ? n : pc;
-  pc = round_up(pc, 32);
-  const int64_t pp = round_up(P, 32);
+  pc = round_up(pc, 64);
+  const int64_t pp = round_up(P, 64);
   if (5 * pc > (int64_t)INT32_MAX - kBM) return fail(c, QMCKL_FAILURE_DEVICE, fn, "problem too large for the split-BF16 form");
   qmckl_exit_code_device rc = ensure_tables(ctx, c);
   if (rc != QMCKL_SUCCESS_DEVICE) return rc;
@@ -1145,7 +1148,7 @@ qmckl_exit_code_device split_mo_vgl_to_host(Ctx* ctx, qmckl_context_device c, do
     for (int k = 0; k < nc; ++k) {
       const int64_t n = sizes[k];
       bounds[k] = off;
-      hj.tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 32), n, ao.point_perm + off,
+      hj.tiles[k] = make_job_mn(jobs[k], ap, round_up(n, 64), n, ao.point_perm + off,
                                 static_cast<const __nv_bfloat16*>(mo.coef_split), M, kp, mo.mo_vgl + 5 * off * M, 0);
       if (hj.tiles[k] < 0) return fail(c, QMCKL_FAILURE_DEVICE, fn, "cuTensorMapEncodeTiled failed");
       off += n;
