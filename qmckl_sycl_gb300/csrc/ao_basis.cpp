@@ -311,7 +311,9 @@ qmckl_exit_code_device build_tables(Ctx* ctx, qmckl_context_device c) {
       se.prim_end = (int32_t)t.h_prims.size();
       se.ao_begin = ao_counter;
       se.l = (int16_t)l;
-      se.orig = 0;
+      se.unit_aof = 1;
+      for (int i = 0; i < ncart(l); ++i)
+        if (ao_counter + i >= A || !(aof[(size_t)(ao_counter + i)] == 1.0)) se.unit_aof = 0;
       ao_counter += ncart(l);
       e.lmax = std::max(e.lmax, l);
       w += (double)spn[s] + 0.5 * ncart(l);

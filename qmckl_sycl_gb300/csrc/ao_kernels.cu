@@ -558,40 +558,49 @@ __device__ __forceinline__ void cart(Writer<O>& w, const Pows& pw, const ShellVa
   w.emit(v);
 }
 
+// The AO factor of AO i: 1 without a load when the shell's factors are all exactly 1 (unit is
+// warp-uniform; the load is predicated, so no code is duplicated).
+__device__ __forceinline__ double ao_factor_at(const double* __restrict__ aof, int i, bool unit) {
+  double f = 1.0;
+  if (!unit) f = __ldg(aof + i);
+  return f;
+}
+
 // Components of one shell in the reference's order: a descending, then b descending
 // (src/qmckl_ao_sycl.cpp:297-305).
 template <Out O, int L>
 __device__ __forceinline__ void shell_fixed(Writer<O>& w, const Pows& pw, const ShellVals& sv_in,
-                                            const double* __restrict__ aof, int ao0, bool zero, const PolyZero& pz) {
+                                            const double* __restrict__ aof, int ao0, bool unit, bool zero,
+                                            const PolyZero& pz) {
   ShellVals s = sv_in;
   if constexpr (O == Out::Planes && L >= 2) {
     s.R2f = s.Rf + s.Rf;  // exact
     if constexpr (L >= 3) s.R6f = 3.f * s.R2f;
   }
   if constexpr (L == 0) {
-    cart<O, 0, 0, 0>(w, pw, s, __ldg(aof + ao0), zero, pz);
+    cart<O, 0, 0, 0>(w, pw, s, ao_factor_at(aof, ao0, unit), zero, pz);
   } else if constexpr (L == 1) {
-    cart<O, 1, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero, pz);
-    cart<O, 0, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero, pz);
-    cart<O, 0, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero, pz);
+    cart<O, 1, 0, 0>(w, pw, s, ao_factor_at(aof, ao0 + 0, unit), zero, pz);
+    cart<O, 0, 1, 0>(w, pw, s, ao_factor_at(aof, ao0 + 1, unit), zero, pz);
+    cart<O, 0, 0, 1>(w, pw, s, ao_factor_at(aof, ao0 + 2, unit), zero, pz);
   } else if constexpr (L == 2) {
-    cart<O, 2, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero, pz);
-    cart<O, 1, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero, pz);
-    cart<O, 1, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero, pz);
-    cart<O, 0, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero, pz);
-    cart<O, 0, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero, pz);
-    cart<O, 0, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero, pz);
+    cart<O, 2, 0, 0>(w, pw, s, ao_factor_at(aof, ao0 + 0, unit), zero, pz);
+    cart<O, 1, 1, 0>(w, pw, s, ao_factor_at(aof, ao0 + 1, unit), zero, pz);
+    cart<O, 1, 0, 1>(w, pw, s, ao_factor_at(aof, ao0 + 2, unit), zero, pz);
+    cart<O, 0, 2, 0>(w, pw, s, ao_factor_at(aof, ao0 + 3, unit), zero, pz);
+    cart<O, 0, 1, 1>(w, pw, s, ao_factor_at(aof, ao0 + 4, unit), zero, pz);
+    cart<O, 0, 0, 2>(w, pw, s, ao_factor_at(aof, ao0 + 5, unit), zero, pz);
   } else {
-    cart<O, 3, 0, 0>(w, pw, s, __ldg(aof + ao0 + 0), zero, pz);
-    cart<O, 2, 1, 0>(w, pw, s, __ldg(aof + ao0 + 1), zero, pz);
-    cart<O, 2, 0, 1>(w, pw, s, __ldg(aof + ao0 + 2), zero, pz);
-    cart<O, 1, 2, 0>(w, pw, s, __ldg(aof + ao0 + 3), zero, pz);
-    cart<O, 1, 1, 1>(w, pw, s, __ldg(aof + ao0 + 4), zero, pz);
-    cart<O, 1, 0, 2>(w, pw, s, __ldg(aof + ao0 + 5), zero, pz);
-    cart<O, 0, 3, 0>(w, pw, s, __ldg(aof + ao0 + 6), zero, pz);
-    cart<O, 0, 2, 1>(w, pw, s, __ldg(aof + ao0 + 7), zero, pz);
-    cart<O, 0, 1, 2>(w, pw, s, __ldg(aof + ao0 + 8), zero, pz);
-    cart<O, 0, 0, 3>(w, pw, s, __ldg(aof + ao0 + 9), zero, pz);
+    cart<O, 3, 0, 0>(w, pw, s, ao_factor_at(aof, ao0 + 0, unit), zero, pz);
+    cart<O, 2, 1, 0>(w, pw, s, ao_factor_at(aof, ao0 + 1, unit), zero, pz);
+    cart<O, 2, 0, 1>(w, pw, s, ao_factor_at(aof, ao0 + 2, unit), zero, pz);
+    cart<O, 1, 2, 0>(w, pw, s, ao_factor_at(aof, ao0 + 3, unit), zero, pz);
+    cart<O, 1, 1, 1>(w, pw, s, ao_factor_at(aof, ao0 + 4, unit), zero, pz);
+    cart<O, 1, 0, 2>(w, pw, s, ao_factor_at(aof, ao0 + 5, unit), zero, pz);
+    cart<O, 0, 3, 0>(w, pw, s, ao_factor_at(aof, ao0 + 6, unit), zero, pz);
+    cart<O, 0, 2, 1>(w, pw, s, ao_factor_at(aof, ao0 + 7, unit), zero, pz);
+    cart<O, 0, 1, 2>(w, pw, s, ao_factor_at(aof, ao0 + 8, unit), zero, pz);
+    cart<O, 0, 0, 3>(w, pw, s, ao_factor_at(aof, ao0 + 9, unit), zero, pz);
   }
 }
 
@@ -820,10 +829,10 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         sv.t2f = gf * yf;
         sv.t3f = gf * zf;
         switch (S.l) {
-          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
-          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
-          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
-          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
           default:
             if constexpr (G) {  // the generic path assembles in FP64
               const double g64 = pairs ? 2.0 * (f32_to_f64(Gs.h) + f32_to_f64(Gs.l)) : g;
@@ -919,10 +928,10 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         }
         const PolyZero pz{};
         switch (S.l) {
-          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
-          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
-          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
-          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, scr, pz); break;
+          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
           default:
             if constexpr (G) shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
             break;

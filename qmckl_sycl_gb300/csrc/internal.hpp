@@ -53,7 +53,7 @@ struct ShellEntry {        // 16 bytes
   int32_t prim_begin, prim_end;  // range in the packed primitive list
   int32_t ao_begin;
   int16_t l;
-  int16_t orig;            // unused (the original index lives in shell_orig)
+  int16_t unit_aof;        // 1: every AO factor of the shell is exactly 1 (the kernels load none)
 };
 struct PrimEntry {         // 48 bytes
   double expo;
