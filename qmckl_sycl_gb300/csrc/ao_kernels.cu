@@ -744,13 +744,13 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         }
       }
       for (int si = s_begin; si < s_end; ++si) {
-        const ShellEntry S = a.shells[si];
+        const ShellEntry sh = a.shells[si];
         F2 R{0.f, 0.f}, Gs{0.f, 0.f}, Hs{0.f, 0.f};  // sum v, sum -expo v, sum expo^2 v
         double t0 = 0.0, g = 0.0, h = 0.0;           // FP64 sums (basis outside the folded range)
         if (pairs) {
           if (shared_e) {
             const float2* eb = reinterpret_cast<const float2*>(ebuf);
-            for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+            for (int pi = sh.prim_begin; pi < sh.prim_end; ++pi) {
               const FoldRec F = load_fold(a.fold + pi);
               const bool act = !scr && (r2b < F.thr);
               if (__any_sync(kFull, act)) {
@@ -761,7 +761,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
               }
             }
           } else {
-            for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+            for (int pi = sh.prim_begin; pi < sh.prim_end; ++pi) {
               const FoldRec F = load_fold(a.fold + pi);
               const bool act = !scr && (r2b < F.thr);
               if (__any_sync(kFull, act)) {
@@ -772,7 +772,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
             }
           }
         } else {
-          for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+          for (int pi = sh.prim_begin; pi < sh.prim_end; ++pi) {
             const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
             if (__any_sync(kFull, act)) {
               const double ar2 = __ldg(&a.prims[pi].expo) * r2;
@@ -788,7 +788,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         if (nan_warp) {
           // every primitive of a NaN lane is NaN in the reference; the outputs follow by arithmetic
           // (the FP32 quantities become NaN, and so does the contraction)
-          if (nanr && S.prim_end > S.prim_begin) {
+          if (nanr && sh.prim_end > sh.prim_begin) {
             R.h = Gs.h = Hs.h = __uint_as_float(0x7FC00000u);
             t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
           }
@@ -800,7 +800,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
                                     __float_as_uint(Gs.l) | __float_as_uint(Hs.h) | __float_as_uint(Hs.l)) << 1) != 0
                                 : ((bits_of(t0) | bits_of(g) | bits_of(h)) << 1) != 0;
           if (!__any_sync(kFull, nz)) {
-            w.emit_zeros((S.l + 1) * (S.l + 2) / 2);
+            w.emit_zeros((sh.l + 1) * (sh.l + 2) / 2);
             continue;
           }
         }
@@ -813,13 +813,13 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
           // cancellation-prone part of the Laplacian, in pair arithmetic before one rounding
           sv.Rf = __fadd_rn(R.h, R.l);
           gf = 2.f * __fadd_rn(Gs.h, Gs.l);
-          rt = mul_pair((float)(3 + 2 * S.l), 0.f, Gs.h, Gs.l);
+          rt = mul_pair((float)(3 + 2 * sh.l), 0.f, Gs.h, Gs.l);
           const F2 rh = mul_pair(r2h, r2l, Hs.h, Hs.l);
           add_pair(rt, F2{2.f * rh.h, 2.f * rh.l});
           sv.Rtf = 2.f * __fadd_rn(rt.h, rt.l);
           sv.rzero = R.h == -R.l;  // the FP64 value R.h + R.l is zero
         } else {
-          Rt = fma(kTwoL[S.l], g, fma(-2.0, h, 3.0 * g));
+          Rt = fma(kTwoL[sh.l], g, fma(-2.0, h, 3.0 * g));
           sv.Rf = f64_to_f32(t0);
           gf = f64_to_f32(g);
           sv.Rtf = f64_to_f32(Rt);
@@ -828,11 +828,11 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         sv.t1f = gf * xf;
         sv.t2f = gf * yf;
         sv.t3f = gf * zf;
-        switch (S.l) {
-          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
-          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
-          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
-          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+        switch (sh.l) {
+          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, xf, yf, zf), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
+          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, xf, yf, zf), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
+          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, xf, yf, zf), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
+          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, xf, yf, zf), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
           default:
             if constexpr (G) {  // the generic path assembles in FP64
               const double g64 = pairs ? 2.0 * (f32_to_f64(Gs.h) + f32_to_f64(Gs.l)) : g;
@@ -841,7 +841,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
               sv.t1 = g64 * x;
               sv.t2 = g64 * y;
               sv.t3 = g64 * z;
-              shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
+              shell_generic<O>(w, x, y, z, sh.l, sv, a.aof, sh.ao_begin, scr);
             }
             break;
         }
@@ -867,10 +867,10 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         }
       }
       for (int si = s_begin; si < s_end; ++si) {
-        const ShellEntry S = a.shells[si];
+        const ShellEntry sh = a.shells[si];
         double t0 = 0.0, g = 0.0, h = 0.0;
         if (shared_e) {
-          for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+          for (int pi = sh.prim_begin; pi < sh.prim_end; ++pi) {
             const PrimEntry* P = a.prims + pi;
             const bool act = !scr && (r2b < __ldg(&P->thr_bits));
             if (__any_sync(kFull, act)) {
@@ -886,7 +886,7 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
             }
           }
         } else {
-          for (int pi = S.prim_begin; pi < S.prim_end; ++pi) {
+          for (int pi = sh.prim_begin; pi < sh.prim_end; ++pi) {
             const bool act = !scr && (r2b < __ldg(&a.prims[pi].thr_bits));
             if (__any_sync(kFull, act)) {
               const double expo = __ldg(&a.prims[pi].expo);
@@ -905,11 +905,11 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
         }
         if (nan_warp) {
           // every primitive of a NaN lane is NaN in the reference; the outputs follow by arithmetic
-          if (nanr && S.prim_end > S.prim_begin) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
+          if (nanr && sh.prim_end > sh.prim_begin) t0 = g = h = __longlong_as_double(0x7FF8000000000000ll);
         } else if (kSkipDead && !__any_sync(kFull, ((bits_of(t0) | bits_of(g) | bits_of(h)) << 1) != 0)) {
           // no lane has a nonzero radial sum: the shell's AOs are zero in every component,
           // written without the assembly
-          w.emit_zeros((S.l + 1) * (S.l + 2) / 2);
+          w.emit_zeros((sh.l + 1) * (sh.l + 2) / 2);
           continue;
         }
         ShellVals sv;
@@ -920,20 +920,20 @@ __device__ __forceinline__ void ao_task_at(const FusedArgs& a, int64_t group, co
           sv.t3 = g * z;
           // a shell without primitives has a zero radial gradient in the reference, also at a NaN
           // coordinate (where g * x would be NaN)
-          if (nan_warp && nanr && S.prim_end == S.prim_begin) sv.t1 = sv.t2 = sv.t3 = 0.0;
+          if (nan_warp && nanr && sh.prim_end == sh.prim_begin) sv.t1 = sv.t2 = sv.t3 = 0.0;
           const double t4 = fma(-2.0, h, 3.0 * g);
-          sv.Rt = fma(kTwoL[S.l], g, t4);
+          sv.Rt = fma(kTwoL[sh.l], g, t4);
         } else {
           sv.t1 = sv.t2 = sv.t3 = sv.Rt = 0.0;
         }
         const PolyZero pz{};
-        switch (S.l) {
-          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
-          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
-          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
-          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, S.ao_begin, S.unit_aof != 0, scr, pz); break;
+        switch (sh.l) {
+          case 0: shell_fixed<O, 0>(w, make_pows<O, 0>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
+          case 1: shell_fixed<O, 1>(w, make_pows<O, 1>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
+          case 2: shell_fixed<O, 2>(w, make_pows<O, 2>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
+          case 3: shell_fixed<O, 3>(w, make_pows<O, 3>(x, y, z, 0.f, 0.f, 0.f), sv, a.aof, sh.ao_begin, sh.unit_aof != 0, scr, pz); break;
           default:
-            if constexpr (G) shell_generic<O>(w, x, y, z, S.l, sv, a.aof, S.ao_begin, scr);
+            if constexpr (G) shell_generic<O>(w, x, y, z, sh.l, sv, a.aof, sh.ao_begin, scr);
             break;
         }
       }
