@@ -27,8 +27,8 @@ def _replace(s, **kw):
 
 
 def _unfoldable():
-    # a coefficient outside the folded evaluation's range (2^-900): the planes kernel evaluates
-    # the radials like the FP64 form
+    # a coefficient outside the folded evaluation's range (binary exponent beyond +-64): the planes
+    # kernel evaluates the radials like the FP64 form
     s = config_small(6, point_num=200)
     c = s.coefficient.copy()
     c[3] = 1e-300
@@ -66,6 +66,31 @@ def test_split_respects_zero_value_skip():
     ref = oracle.forward(s, want=("mo_vgl",))
     out = run(s, PRECISION_SPLIT_BF16)
     assert normwise_rel_err(out["mo_vgl"], ref["mo_vgl"]) <= MIXED_RTOL
+
+
+def test_split_tiny_displacements():
+    # Displacements below 2^-340 can underflow the FP64 polynomial x^a (y^b z^c), which the
+    # reference's zero-value skip tests (src/qmckl_mo_sycl.cpp:40); the split form then decides
+    # that skip from the FP64 product itself (a warp-uniform branch) instead of the displacements'
+    # zero tests. Nucleus 0 sits on the plane x = 0 so that the displacements are the points' own
+    # tiny coordinates: 1e-200, 3e-300 and a subnormal one, mixed with ordinary points in one warp.
+    s = config_small(4, point_num=64)
+    nc = s.nucl_coord.copy()
+    nc[0, 0] = 0.0
+    coord = s.coord.copy()
+    coord[:16, 0] = 1e-200
+    coord[16:24, 0] = -3e-300
+    coord[24:28, 0] = 5e-320
+    coord[28:32, 0] = 0.0
+    s = _replace(s, nucl_coord=nc).with_points(coord)
+    ref = oracle.forward(s, want=("ao_vgl", "mo_vgl", "mo_value"))
+    plain = run(s, PRECISION_FP64)
+    assert np.array_equal(plain["ao_vgl"] == 0.0, ref["ao_vgl"] == 0.0)
+    assert normwise_rel_err(plain["mo_vgl"], ref["mo_vgl"]) <= 1e-12
+    out = run(s, PRECISION_SPLIT_BF16)
+    errs = [normwise_rel_err(out["mo_vgl"][:, c:c + 1], ref["mo_vgl"][:, c:c + 1]) for c in range(5)]
+    assert max(errs) <= MIXED_RTOL
+    assert normwise_rel_err(out["mo_value"], ref["mo_value"]) <= MIXED_RTOL
 
 
 def test_mode_switch_recomputes(chbrclf):
