@@ -310,10 +310,13 @@ qmckl_exit_code_device qmckl_get_mo_basis_mo_value_inplace_device(qmckl_context_
 
 /* MO contraction precision. FP64 (default, the drop-in) or a split-BF16 product on the
  * tcgen05 tensor cores (each operand split into three BF16 terms, six cross products, FP32
- * accumulation with per-block two-sum folding). Distances, exponentials, radial sums,
- * screening and the AO Laplacian assembly stay FP64 in both modes; in the split-BF16 mode the
- * AO value and gradient are assembled in FP32 (the BF16 planes carry 24 significant bits).
- * The AO getters always return the FP64 AOs. Changing the mode touches the context. */
+ * accumulation with per-block two-sum folding). The displacements, r2 and the screening
+ * decisions are FP64 in both modes; in the split-BF16 mode the AO operand carries 24
+ * significant bits, so its primitives and radial sums run in FP32 pair arithmetic (about 44
+ * bits, within 2e-10 relative of the exact primitive values) and its AO components are
+ * assembled in FP32, while the reference's zero-value skip keeps its FP64 decisions. A basis
+ * with a coefficient beyond 2^+-64 or an exponent beyond 2^+-60 takes the FP64 radials in that
+ * mode too. The AO getters always return the FP64 AOs. Changing the mode touches the context. */
 #define QMCKL_PRECISION_FP64_DEVICE 0
 #define QMCKL_PRECISION_SPLIT_BF16_DEVICE 1
 qmckl_exit_code_device qmckl_set_precision_mode_device(qmckl_context_device context, int32_t mode);
