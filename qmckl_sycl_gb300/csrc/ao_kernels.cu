@@ -54,8 +54,14 @@ constexpr int kWarps = 4;          // warps per CTA (each runs its own task)
 #ifndef QMCKL_AO_TASKS_PER_WARP
 #define QMCKL_AO_TASKS_PER_WARP 2
 #endif
-// Tasks per resident warp the nucleus-chunk level is chosen for (finer chunks give more tasks).
+#ifndef QMCKL_AO_PLANES_TASKS_PER_WARP
+#define QMCKL_AO_PLANES_TASKS_PER_WARP 1
+#endif
+// Tasks per resident warp the nucleus-chunk level is chosen for (finer chunks give more tasks):
+// 2 for the FP64 outputs; 1 for the split-BF16 planes, whose FP32 radials make a task about half
+// as long (planes on the medium workload 0.446 ms against 0.455 ms with 2 and 0.497 ms with 4).
 constexpr int kTasksPerWarp = QMCKL_AO_TASKS_PER_WARP;
+constexpr int kPlanesTasksPerWarp = QMCKL_AO_PLANES_TASKS_PER_WARP;
 #ifndef QMCKL_AO_TAIL_SEGMENTS
 #define QMCKL_AO_TAIL_SEGMENTS 8
 #endif
@@ -1211,10 +1217,11 @@ cudaError_t launch_fused_g(Ctx* ctx, const AoTables& t, const double* coord, con
   constexpr bool kPieces = O == Out::Planes;  // the FP64 outputs never take pieces (see pick_level)
   const int per_sm = cached_per_sm;
   const int64_t resident_warps = (int64_t)t.sm_count * per_sm * kWarps;
-  // two or more tasks per resident warp, taken from a counter: with one task per warp the SMs
-  // that receive one CTA more than the others set the time (4 or 5 CTAs per SM on the medium
-  // workload, 16 % idle FP64 issue)
-  const int level = pick_level(t, groups, kTasksPerWarp * resident_warps, kPieces);
+  // tasks taken from a counter, two or more per resident warp for the FP64 outputs: with one task
+  // per warp the SMs that receive one CTA more than the others set the time (4 or 5 CTAs per SM on
+  // the medium workload, 16 % idle FP64 issue); the planes' shorter tasks balance with one
+  const int level = pick_level(t, groups, (O == Out::Planes ? kPlanesTasksPerWarp : kTasksPerWarp) * resident_warps,
+                               kPieces);
   FusedArgs a = make_fused_args(t, level, coord, perm, point_num, out, planes, row_len);
   // the last tasks at ever finer nucleus-chunk levels: a warp's last task is short, so the launch
   // ends with every warp busy nearly to the end (a task at the coarse level takes ~1/3 of the
