@@ -1058,7 +1058,8 @@ __global__ void __launch_bounds__(kWarps * 32, min_ctas<O>()) ao_batch_kernel(co
     const int64_t g = local / cn;
     // the FP64 outputs skip shells that are zero on every lane (64-molecule ao_vgl 6.06 -> 5.33 ms);
     // the planes do not: there the test cost the batch kernel more than it saved (2.26 ms without,
-    // 2.38 ms with it, also with the arguments copied to shared memory)
+    // 2.38 ms with it, also with the arguments copied to shared memory; with the FP32 pair radials
+    // 1.392 ms without, 1.434 ms with it)
     ao_task_at<O, G, B, false, O != Out::Planes || kBatchPlanesSkipDead>(a, g, a.chunks + (local - g * cn), sm.st,
                                                                           sm.thi, sm.tlo, sm.fine,
                                                  sm.ebuf, lane);
