@@ -726,6 +726,8 @@ def main():
                     # 16-padded column tiles); the algorithmic figure above counts 10 A M per point
                     out[k]["bf16_products"] = 6
                     out[k]["bf16_work_frac"] = 6.0 * out[k]["frac"]
+                    out[k]["note"] = ("frac counts the algorithmic 10 A M FLOPs per point; the kernel executes "
+                                      "six BF16 products per algorithmic one: bf16_work_frac")
         return out
 
     rf = {f: roof(f) for f in forms}
